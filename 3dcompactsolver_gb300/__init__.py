@@ -1,0 +1,379 @@
+"""GB300 implementation of the per-RK-stage path of 3DCompactSolver.
+
+The compute runs in libcs3d_gb300.so (hand-written sm_103a kernels behind the
+C ABI of include/cs3d.h).  This module binds that ABI with ctypes and mirrors
+the reference's C++ interface for the path under the same names:
+
+    Domain(Nx, Ny, Nz, Lx, Ly, Lz)                      Domain.hpp:16
+    BC(bcXType, bcX0, bcX1, bcYType, ...)               BC.hpp:16
+    TimeStepping(type, CFL, maxTimeStep, maxTime, ...)  TimeStepping.hpp:20
+    CSolver_GB300(dom, bc, ts, alphaF, mu_ref, ...)     CSolver_AWS.hpp:119
+    RK4(cs), TVDRK3(cs)                                 RK4.hpp:7, TVDRK3.hpp:7
+    Derivatives(dom, bcType, dir), Filter(alphaF, ...)  Derivatives.hpp:54, Filter.hpp:31
+
+There is no CPU fallback: if the library is missing or no GPU is visible, the
+constructors raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (  # noqa: F401  (re-exported constants)
+    Config, make_config, PERIODIC_SOLVE, DIRICHLET_SOLVE, PERIODIC, SPONGE, ADIABATIC_WALL,
+    MOVING_ADIABATIC_WALL, INLET, DIRX, DIRY, DIRZ, RK4 as RK4_KIND, TVDRK3 as TVDRK3_KIND, FP64,
+    FP32_MIXED, SPONGE_REFERENCE, SPONGE_BANDS)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcs3d_gb300.so")
+
+OPT_STORE_INCREMENTS = 1
+OPT_STORE_DIAGNOSTICS = 2
+OPT_KERNEL_TIMING = 3
+KERNEL_CLASSES = ("sweep_x", "sweep_y", "sweep_z", "filter", "boundary", "cfl", "sponge", "other")
+
+_lib = None
+_DP = ctypes.POINTER(ctypes.c_double)
+_H = ctypes.c_void_p
+
+
+class CS3DError(RuntimeError):
+    """A status code other than CS3D_OK returned by the C ABI."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; "
+                              "g.build()'` (or 3dcompactsolver_gb300/build.py) first")
+        L = ctypes.CDLL(LIB_PATH)
+        L.cs3d_last_error.restype = ctypes.c_char_p
+        L.cs3d_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(_H)]
+        L.cs3d_destroy.argtypes = [_H]
+        L.cs3d_set_initial_conditions.argtypes = [_H, _DP, _DP, _DP, _DP, _DP]
+        for name in ("cs3d_step", "cs3d_pre_step", "cs3d_post_step", "cs3d_sync"):
+            getattr(L, name).argtypes = [_H]
+        L.cs3d_run.argtypes = [_H, ctypes.c_int]
+        L.cs3d_sub_step.argtypes = [_H, ctypes.c_int, ctypes.c_int]
+        L.cs3d_get_field.argtypes = [_H, ctypes.c_int, _DP]
+        L.cs3d_set_field.argtypes = [_H, ctypes.c_int, _DP]
+        L.cs3d_field_ptr.argtypes = [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.cs3d_get_scalars.argtypes = [_H, _DP, _DP, ctypes.POINTER(ctypes.c_int)]
+        L.cs3d_get_stream.argtypes = [_H, ctypes.POINTER(ctypes.c_void_p)]
+        L.cs3d_launch_count.argtypes = [_H, ctypes.POINTER(ctypes.c_longlong)]
+        L.cs3d_set_option.argtypes = [_H, ctypes.c_int, ctypes.c_int]
+        for name in ("cs3d_deriv1", "cs3d_deriv2", "cs3d_filter"):
+            getattr(L, name).argtypes = [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.cs3d_tgv_quantities.argtypes = [_H, _DP]
+        L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
+                                        ctypes.c_int]
+        L.cs3d_version.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise CS3DError(rc, lib().cs3d_last_error().decode(errors="replace"))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+class Solver:
+    """One solver handle on the current CUDA device (the C ABI, 1:1)."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.shape = (cfg.Nz, cfg.Ny, cfg.Nx)
+        h = _H()
+        check(lib().cs3d_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cs3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_initial_conditions(self, rho0, p0, U0, V0, W0):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (rho0, p0, U0, V0, W0)]
+        for a in arrs:
+            if a.size != self.cfg.npts:
+                raise ValueError(f"initial field has {a.size} points, expected {self.cfg.npts}")
+        check(lib().cs3d_set_initial_conditions(self.h, *[_dptr(a) for a in arrs]))
+
+    def step(self):
+        check(lib().cs3d_step(self.h))
+
+    def run(self, n):
+        check(lib().cs3d_run(self.h, int(n)))
+
+    def pre_step(self):
+        check(lib().cs3d_pre_step(self.h))
+
+    def sub_step(self, rk_step, rk_last):
+        check(lib().cs3d_sub_step(self.h, int(rk_step), int(bool(rk_last))))
+
+    def post_step(self):
+        check(lib().cs3d_post_step(self.h))
+
+    def sync(self):
+        check(lib().cs3d_sync(self.h))
+
+    def set_option(self, option, value=1):
+        check(lib().cs3d_set_option(self.h, option, int(value)))
+
+    def get(self, field):
+        out = np.empty(self.shape, np.float64)
+        check(lib().cs3d_get_field(self.h, int(field), _dptr(out)))
+        return out
+
+    def set(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        check(lib().cs3d_set_field(self.h, int(field), _dptr(a)))
+
+    def field_ptr(self, field):
+        p = ctypes.c_void_p()
+        check(lib().cs3d_field_ptr(self.h, int(field), ctypes.byref(p)))
+        return p.value
+
+    def conserved(self):
+        """q1 as a (5, Nz, Ny, Nx) array."""
+        return np.stack([self.get(_abi.F_RHO1 + f) for f in range(5)])
+
+    def scalars(self):
+        dt, t, ts = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        check(lib().cs3d_get_scalars(self.h, ctypes.byref(dt), ctypes.byref(t), ctypes.byref(ts)))
+        return dt.value, t.value, ts.value
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().cs3d_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def launch_count(self):
+        c = ctypes.c_longlong()
+        check(lib().cs3d_launch_count(self.h, ctypes.byref(c)))
+        return c.value
+
+    def kernel_times(self, reset=False):
+        """{class: (total_ms, launches)} accumulated while OPT_KERNEL_TIMING was on."""
+        n = len(KERNEL_CLASSES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        check(lib().cs3d_kernel_times(self.h, ms, cnt, n, int(reset)))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
+
+    def tgv_quantities(self):
+        out = np.zeros(7)
+        check(lib().cs3d_tgv_quantities(self.h, _dptr(out)))
+        return out
+
+    def line_op(self, kind, direction, in_ptr, out_ptr):
+        """kind 1/2/3 = deriv1/deriv2/filter on device arrays in the direction's
+        contiguous layout."""
+        fn = {1: lib().cs3d_deriv1, 2: lib().cs3d_deriv2, 3: lib().cs3d_filter}[kind]
+        check(fn(self.h, int(direction), ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr)))
+
+
+# ---------------------------------------------------------------------------
+# reference-named interface
+# ---------------------------------------------------------------------------
+class Domain:
+    """Grid of Domain.hpp:16-52: x_i = i*L/(N-1)."""
+
+    def __init__(self, Nx, Ny, Nz, Lx, Ly, Lz):
+        self.Nx, self.Ny, self.Nz = int(Nx), int(Ny), int(Nz)
+        self.N = self.Nx * self.Ny * self.Nz
+        self.Lx, self.Ly, self.Lz = float(Lx), float(Ly), float(Lz)
+        self.x = np.array([(float(i) / (float(self.Nx) - 1.0)) * self.Lx for i in range(self.Nx)])
+        self.y = np.array([(float(j) / (float(self.Ny) - 1.0)) * self.Ly for j in range(self.Ny)])
+        self.z = np.array([(float(k) / (float(self.Nz) - 1.0)) * self.Lz for k in range(self.Nz)])
+        self.dx = self.x[1] - self.x[0]
+        self.dy = self.y[1] - self.y[0]
+        self.dz = self.z[1] - self.z[0]
+
+
+class BC:
+    """Boundary types and kinds of BC.hpp:10-31."""
+    PERIODIC_SOLVE, DIRICHLET_SOLVE = PERIODIC_SOLVE, DIRICHLET_SOLVE
+    PERIODIC, SPONGE, ADIABATIC_WALL, MOVING_ADIABATIC_WALL, INLET = (
+        PERIODIC, SPONGE, ADIABATIC_WALL, MOVING_ADIABATIC_WALL, INLET)
+
+    def __init__(self, bcXType, bcX0, bcX1, bcYType, bcY0, bcY1, bcZType, bcZ0, bcZ1):
+        self.bcXType, self.bcYType, self.bcZType = bcXType, bcYType, bcZType
+        self.bcX0, self.bcX1, self.bcY0, self.bcY1, self.bcZ0, self.bcZ1 = (
+            bcX0, bcX1, bcY0, bcY1, bcZ0, bcZ1)
+
+
+class TimeStepping:
+    """TimeStepping.hpp:10-40.  The reference always steps at constant CFL
+    (CSolver_AWS.cpp:530); dt_fixed > 0 freezes dt instead."""
+    CONST_DT, CONST_CFL = 0, 1
+
+    def __init__(self, timeSteppingType, CFL, maxTimeStep, maxTime, filterStep, checkStep=1,
+                 dumpStep=1 << 30, dt_fixed=0.0):
+        self.timeSteppingType = timeSteppingType
+        self.CFL = float(CFL)
+        self.maxTimeStep = int(maxTimeStep)
+        self.maxTime = float(maxTime)
+        self.filterStep = int(filterStep)
+        self.checkStep = int(checkStep)
+        self.dumpStep = int(dumpStep)
+        self.dt_fixed = float(dt_fixed)
+        self.dt = 0.0
+
+
+class CSolver_GB300:
+    """Drop-in for CSolver_AWS (CSolver_AWS.hpp:119) on one GPU.
+
+    The reference's five stage virtuals run as one fused launch sequence, which
+    is issued by updateData(), the last of them; preSubStep, solveEqnSet and
+    postSubStep only record the call.  Public state arrays (rho1 ... rhoE2,
+    U, V, W, p, T, mu, sos) are read from the device on access."""
+
+    def __init__(self, dom, bc, ts, alphaF, mu_ref, blocksize=16, useTiming=False, rk=_abi.RK4,
+                 precision=FP64, sponge_mode=SPONGE_REFERENCE, sponge_frac=(0.0,) * 6,
+                 wall_vel=(0.0,) * 12):
+        self.dom, self.bc, self.ts = dom, bc, ts
+        self.alphaF, self.mu_ref = float(alphaF), float(mu_ref)
+        self.blocksize, self.useTiming = blocksize, useTiming
+        cfg = make_config(
+            (dom.Nx, dom.Ny, dom.Nz), (dom.Lx, dom.Ly, dom.Lz),
+            bc_type=(bc.bcXType, bc.bcYType, bc.bcZType),
+            bc_kind=(bc.bcX0, bc.bcX1, bc.bcY0, bc.bcY1, bc.bcZ0, bc.bcZ1), alphaF=alphaF,
+            mu_ref=mu_ref, CFL=ts.CFL, filter_step=ts.filterStep, rk=rk, precision=precision,
+            sponge_mode=sponge_mode, sponge_frac=sponge_frac, wall_vel=wall_vel,
+            dt_fixed=ts.dt_fixed)
+        self.solver = Solver(cfg)
+        shape = (dom.Nz, dom.Ny, dom.Nx)
+        self.rho0 = np.ones(shape)
+        self.p0 = np.ones(shape)
+        self.U0 = np.zeros(shape)
+        self.V0 = np.zeros(shape)
+        self.W0 = np.zeros(shape)
+        self.rkStep, self.rkLast, self.endFlag = 1, False, False
+        self.timeStep, self.time = 0, 0.0
+
+    # AbstractCSolver.hpp:36-43
+    def initializeSolverData(self):
+        pass  # device arrays are allocated by the constructor
+
+    def setInitialConditions(self):
+        self.solver.set_initial_conditions(self.rho0, self.p0, self.U0, self.V0, self.W0)
+
+    def preStep(self):
+        self.solver.pre_step()
+        self.timeStep += 1
+
+    def preSubStep(self):
+        pass
+
+    def solveEqnSet(self):
+        pass
+
+    def postSubStep(self):
+        pass
+
+    def updateData(self):
+        self.solver.sub_step(self.rkStep, self.rkLast)
+
+    def postStep(self):
+        self.solver.post_step()
+        if self.timeStep >= self.ts.maxTimeStep:
+            self.endFlag = True
+        elif self.ts.maxTime < 1e300:
+            _, t, _ = self.solver.scalars()
+            self.time = t
+            if t >= self.ts.maxTime:
+                self.endFlag = True
+
+    def __getattr__(self, name):
+        fields = {"rho1": 0, "rhoU1": 1, "rhoV1": 2, "rhoW1": 3, "rhoE1": 4, "rhok": 5, "rhoUk": 6,
+                  "rhoVk": 7, "rhoWk": 8, "rhoEk": 9, "rho2": 10, "rhoU2": 11, "rhoV2": 12,
+                  "rhoW2": 13, "rhoE2": 14, "rhok2": 15, "rhoUk2": 16, "rhoVk2": 17, "rhoWk2": 18,
+                  "rhoEk2": 19, "U": 20, "V": 21, "W": 22, "p": 23, "T": 24, "mu": 25, "sos": 26}
+        if name in fields:
+            return self.__dict__["solver"].get(fields[name])
+        raise AttributeError(name)
+
+
+class _RKBase:
+    nstages = 4
+
+    def __init__(self, cs):
+        self.cs = cs
+
+    def updateConservedData(self):
+        pass  # fused into the stage launched by cs.updateData()
+
+    def executeSolverLoop(self):
+        """RK4.hpp:120-170 / TVDRK3.hpp:98-139."""
+        cs = self.cs
+        cs.setInitialConditions()
+        while not cs.endFlag:
+            cs.rkLast = False
+            cs.preStep()
+            for s in range(1, self.nstages + 1):
+                cs.rkStep = s
+                cs.rkLast = s == self.nstages
+                cs.preSubStep()
+                cs.solveEqnSet()
+                cs.postSubStep()
+                self.updateConservedData()
+                cs.updateData()
+            cs.postStep()
+
+
+class RK4(_RKBase):
+    nstages = 4
+
+
+class TVDRK3(_RKBase):
+    nstages = 3
+
+
+class Derivatives:
+    """Derivatives(dom, bcType, dir): calc1stDerivField / calc2ndDerivField on
+    device arrays (integer device addresses) in the direction's contiguous
+    layout (Derivatives.cpp:3-96).  A private solver handle carries the
+    precomputed operators."""
+    DIRX, DIRY, DIRZ = DIRX, DIRY, DIRZ
+
+    def __init__(self, dom, bcType, currentDir, alphaF=0.49):
+        bt = [PERIODIC_SOLVE] * 3
+        bt[currentDir] = bcType
+        cfg = make_config((dom.Nx, dom.Ny, dom.Nz), (dom.Lx, dom.Ly, dom.Lz), bc_type=tuple(bt),
+                          alphaF=alphaF)
+        self.solver = Solver(cfg)
+        self.currentDir = currentDir
+
+    def calc1stDerivField(self, dataIn, dataOut):
+        self.solver.line_op(1, self.currentDir, dataIn, dataOut)
+
+    def calc2ndDerivField(self, dataIn, dataOut):
+        self.solver.line_op(2, self.currentDir, dataIn, dataOut)
+
+
+class Filter(Derivatives):
+    """Filter(alphaF, dom, bcType, dir).filterField (Filter.cpp:129-171)."""
+
+    def __init__(self, alphaF, dom, bcType, currentDir):
+        super().__init__(dom, bcType, currentDir, alphaF=alphaF)
+
+    def filterField(self, dataIn, dataOut):
+        self.solver.line_op(3, self.currentDir, dataIn, dataOut)

@@ -1,0 +1,1034 @@
+// cs3d_abi.cu -- C ABI of the GB300 stage path: solver handle, device memory,
+// precomputed line operators and the order of launches of one time step.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/cs3d.h"
+#include "cs3d_dev.cuh"
+#include "cs3d_kernels.cuh"
+
+using namespace cs3d;
+
+// ---------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+static int fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CS3D_CUDA(call)                                                                           \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(CS3D_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" const char *cs3d_last_error(void) { return g_err; }
+
+extern "C" int cs3d_version(int *major, int *minor, int *sm_arch) {
+    if (major) *major = 1;
+    if (minor) *minor = 0;
+    if (sm_arch) *sm_arch = 103;
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// compact operator coefficients (Derivatives.hpp:79-161, Filter.hpp:54-104)
+// ---------------------------------------------------------------------
+namespace {
+
+struct HostOp {
+    std::vector<double> m, iw, c, z;
+    double taps[kTaps] = {0};
+    double btaps[2 * kMaxH][kTaps] = {{0}};
+    int boff[2 * kMaxH] = {0};
+    double scale = 1.0, bog = 0.0, inv_den = 0.0;
+    int N = 0, H = 2, periodic = 1;
+};
+
+// Thomas algorithm exactly as Utils.cpp:4-20, for the Sherman-Morrison vector.
+void thomas(const std::vector<double> &a, const std::vector<double> &b, const std::vector<double> &c,
+            const std::vector<double> &d, std::vector<double> &x) {
+    int n = (int)b.size();
+    std::vector<double> w(b);
+    x = d;
+    for (int i = 1; i < n; i++) {
+        double mm = a[i] / w[i - 1];
+        w[i] = w[i] - mm * c[i - 1];
+        x[i] = x[i] - mm * x[i - 1];
+    }
+    x[n - 1] /= w[n - 1];
+    for (int i = n - 2; i >= 0; i--) x[i] = (x[i] - c[i] * x[i + 1]) / w[i];
+}
+
+// kind: 1 = first derivative, 2 = second derivative, 3 = filter.
+HostOp make_op(int kind, int N, int bc, double dh, double alphaF) {
+    HostOp op;
+    op.N = N;
+    op.periodic = bc == CS3D_PERIODIC_SOLVE;
+    op.H = kind == 3 ? 4 : 2;
+    std::vector<double> lo(N), di(N, 1.0), up(N);
+    double alpha;
+    // interior coefficients
+    const double a1 = 14.0 / 9.0, b1 = 1.0 / 9.0;                 // Derivatives.hpp:81-83
+    const double a2 = 12.0 / 11.0, b2 = 3.0 / 11.0;               // :101-103
+    double t[kTaps] = {0};
+    if (kind == 1) {
+        alpha = 1.0 / 3.0;
+        t[2] = -b1 / 4.0; t[3] = -a1 / 2.0; t[5] = a1 / 2.0; t[6] = b1 / 4.0;  // Derivatives.cpp:121-124
+        op.scale = 1.0 / dh;
+    } else if (kind == 2) {
+        alpha = 2.0 / 11.0;
+        t[2] = b2 / 4.0; t[3] = a2; t[4] = -(b2 / 2.0 + 2.0 * a2); t[5] = a2; t[6] = b2 / 4.0;  // :155-159
+        op.scale = 1.0 / (dh * dh);
+    } else {
+        alpha = alphaF;
+        // Filter.hpp:54-58, Filter.cpp:7-11
+        double a0_8 = (93.0 + 70.0 * alphaF) / 128.0, a1_8 = (7.0 + 18.0 * alphaF) / 16.0;
+        double a2_8 = (-7.0 + 14.0 * alphaF) / 32.0, a3_8 = (1.0 - 2.0 * alphaF) / 16.0;
+        double a4_8 = (-1.0 + 2.0 * alphaF) / 128.0;
+        double cc[5] = {a0_8, a1_8 / 2.0, a2_8 / 2.0, a3_8 / 2.0, a4_8 / 2.0};
+        for (int k = 0; k <= 4; k++) { t[4 + k] = cc[k]; t[4 - k] = cc[k]; }
+        op.scale = 1.0;
+    }
+    for (int i = 0; i < N; i++) { lo[i] = alpha; up[i] = alpha; }
+    std::memcpy(op.taps, t, sizeof(t));
+    const int H = op.H;
+    if (op.periodic) {
+        for (int b = 0; b < 2 * H; b++) {
+            int row = b < H ? b : N - 2 * H + b;
+            std::memcpy(op.btaps[b], t, sizeof(t));
+            op.boff[b] = row - kMaxH;
+        }
+        // cyclic system (Utils.cpp:22-46): gamma = -b0, modified corners
+        double gamma = -di[0];
+        std::vector<double> bb(di);
+        bb[0] = di[0] - gamma;
+        bb[N - 1] = di[N - 1] - alpha * alpha / gamma;
+        std::vector<double> u(N, 0.0);
+        u[0] = gamma;
+        u[N - 1] = alpha;
+        thomas(lo, bb, up, u, op.z);
+        op.bog = alpha / gamma;
+        op.inv_den = 1.0 / (1.0 + op.z[0] + alpha * op.z[N - 1] / gamma);
+        di = bb;
+    } else {
+        auto set = [&](int b, int off, std::initializer_list<double> v) {
+            int k = 0;
+            for (double x : v) op.btaps[b][k++] = x;
+            op.boff[b] = off;
+        };
+        if (kind == 1) {
+            // Derivatives.hpp:85-97, Derivatives.cpp:191-205
+            const double A1 = -197.0 / 60.0, B1 = -5.0 / 12.0, C1 = 5.0, D1 = -5.0 / 3.0, E1 = 5.0 / 12.0,
+                         F1 = -1.0 / 20.0;
+            const double A2 = -43.0 / 96.0, B2 = -5.0 / 6.0, C2 = 9.0 / 8.0, D2 = 1.0 / 6.0, E2 = -1.0 / 96.0;
+            set(0, 0, {A1, B1, C1, D1, E1, F1});
+            set(1, 0, {A2, B2, C2, D2, E2});
+            set(2, N - 5, {-E2, -D2, -C2, -B2, -A2});
+            set(3, N - 6, {-F1, -E1, -D1, -C1, -B1, -A1});
+            up[0] = 5.0; up[1] = 3.0 / 4.0; lo[1] = 1.0 / 8.0;        // Derivatives.hpp:145-151
+            lo[N - 1] = 5.0; lo[N - 2] = 3.0 / 4.0; up[N - 2] = 1.0 / 8.0;
+        } else if (kind == 2) {
+            // Derivatives.hpp:106-120, Derivatives.cpp:225-240
+            const double A1 = 145.0 / 12.0, B1 = -76.0 / 3.0, C1 = 29.0 / 2.0, D1 = -4.0 / 3.0, E1 = 1.0 / 12.0;
+            const double A2 = 177.0 / 88.0, B2 = -507.0 / 44.0, C2 = 783.0 / 44.0, D2 = -201.0 / 22.0,
+                         E2 = 81.0 / 88.0, F2 = -3.0 / 44.0;
+            set(0, 0, {A1, B1, C1, D1, E1});
+            set(1, 0, {A2, B2, C2, D2, E2, F2});
+            set(2, N - 6, {F2, E2, D2, C2, B2, A2});
+            set(3, N - 5, {E1, D1, C1, B1, A1});
+            up[0] = 10.0; up[1] = -131.0 / 22.0; lo[1] = 2.0 / 11.0;  // Derivatives.hpp:153-159
+            lo[N - 1] = 10.0; lo[N - 2] = -131.0 / 22.0; up[N - 2] = 2.0 / 11.0;
+        } else {
+            // Filter.hpp:60-81, Filter.cpp:64-89
+            double a0_6 = (11.0 + 10.0 * alphaF) / 16.0, a1_6 = (15.0 + 34.0 * alphaF) / 32.0;
+            double a2_6 = (-3.0 + 6.0 * alphaF) / 16.0, a3_6 = (1.0 - 2.0 * alphaF) / 32.0;
+            double aa0 = a0_6, aa1 = a1_6 / 2.0, aa2 = a2_6 / 2.0, aa3 = a3_6 / 2.0;
+            const double A0 = 15.0 / 16.0, A1 = 4.0 / 16.0, A2 = -6.0 / 16.0, A3 = 4.0 / 16.0, A4 = -1.0 / 16.0;
+            const double B0 = 1.0 / 16.0, B1 = 3.0 / 4.0, B2 = 6.0 / 16.0, B3 = -4.0 / 16.0, B4 = 1.0 / 16.0;
+            const double C0 = -1.0 / 16.0, C1 = 4.0 / 16.0, C2 = 5.0 / 8.0, C3 = 4.0 / 16.0, C4 = -1.0 / 16.0;
+            set(0, 0, {A0, A1, A2, A3, A4});
+            set(1, 0, {B0, B1, B2, B3, B4});
+            set(2, 0, {C0, C1, C2, C3, C4});
+            set(3, 0, {aa3, aa2, aa1, aa0, aa1, aa2, aa3});
+            set(4, N - 7, {aa3, aa2, aa1, aa0, aa1, aa2, aa3});
+            set(5, N - 5, {C4, C3, C2, C1, C0});
+            set(6, N - 5, {B4, B3, B2, B1, B0});
+            set(7, N - 5, {A4, A3, A2, A1, A0});
+            for (int r = 0; r < 3; r++) {  // Filter.hpp:89-104
+                lo[r] = 0.0; up[r] = 0.0;
+                lo[N - 1 - r] = 0.0; up[N - 1 - r] = 0.0;
+            }
+        }
+    }
+    // Thomas factors of the (possibly corner-modified) matrix
+    op.m.assign(N, 0.0);
+    op.iw.assign(N, 0.0);
+    op.c = up;
+    std::vector<double> w(di);
+    for (int i = 1; i < N; i++) {
+        op.m[i] = lo[i] / w[i - 1];
+        w[i] = w[i] - op.m[i] * up[i - 1];
+    }
+    for (int i = 0; i < N; i++) op.iw[i] = 1.0 / w[i];
+    if (!op.periodic) op.z.assign(N, 0.0);
+    return op;
+}
+
+// Device copy of an operator in precision T.
+template <typename T>
+struct DevOp {
+    T *mem = nullptr;
+    LineOp<T> op{};
+};
+
+template <typename T>
+int upload_op(const HostOp &h, DevOp<T> &d, cudaStream_t s) {
+    int N = h.N;
+    std::vector<T> buf(4 * (size_t)N);
+    for (int i = 0; i < N; i++) {
+        buf[i] = (T)h.m[i];
+        buf[N + i] = (T)h.iw[i];
+        buf[2 * N + i] = (T)h.c[i];
+        buf[3 * N + i] = (T)h.z[i];
+    }
+    CS3D_CUDA(cudaMalloc(&d.mem, sizeof(T) * 4 * (size_t)N));
+    CS3D_CUDA(cudaMemcpyAsync(d.mem, buf.data(), sizeof(T) * 4 * (size_t)N, cudaMemcpyHostToDevice, s));
+    CS3D_CUDA(cudaStreamSynchronize(s));
+    LineOp<T> &o = d.op;
+    o.m = d.mem;
+    o.iw = d.mem + N;
+    o.c = d.mem + 2 * N;
+    o.z = d.mem + 3 * N;
+    for (int k = 0; k < kTaps; k++) o.taps[k] = (T)h.taps[k];
+    for (int b = 0; b < 2 * kMaxH; b++) {
+        for (int k = 0; k < kTaps; k++) o.btaps[b][k] = (T)h.btaps[b][k];
+        o.boff[b] = h.boff[b];
+    }
+    o.scale = (T)h.scale;
+    o.bog = h.bog;
+    o.inv_den = h.inv_den;
+    o.N = N;
+    o.H = h.H;
+    o.periodic = h.periodic;
+    return CS3D_OK;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------
+// the handle
+// ---------------------------------------------------------------------
+struct cs3d_handle {
+    cs3d_config cfg;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    Geom g{};
+    GasParams gas{};
+    double dx = 0, dy = 0, dz = 0;
+    int nstages = 4;
+    int mixed = 0;
+    size_t tb = 8;  // bytes of the work type
+    // conserved state
+    Q5 q1{}, qk{}, q2{};
+    double *dq[5] = {};
+    // work-precision fields (double or float, by tb)
+    void *prim[5] = {}, *mu = nullptr, *amu = nullptr, *dx4[4] = {}, *dy4[4] = {}, *R[5] = {}, *diag[3] = {};
+    // filter temporaries (work precision) and FP64 temporaries of the plain form
+    void *ft1[5] = {}, *ft2[5] = {};
+    double fref[5] = {0, 0, 0, 0, 0};
+    // sponge
+    int sponge = 0;
+    double *sigma = nullptr;
+    Q5 savg{}, backup{};
+    int backup_valid = 0;
+    int wall_faces = 0, sponge_kind_faces = 0;
+    // scalars on device: dt, time, cfl max, nan flag
+    double *scal = nullptr;
+    int *flag = nullptr;
+    // operators: [dir][kind-1]
+    DevOp<double> op64[3][3];
+    DevOp<float> op32[3][3];
+    // tiles
+    int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads = 128;
+    // step state
+    int timeStep = 0, filterTimeStep = 0;
+    int ic_done = 0;
+    int store_dq = 0, store_diag = 0;
+    long long launches = 0;
+    // optional per-kernel timing with CUDA events on the handle's stream
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    double k_ms[CS3D_NUM_KERNEL_CLASSES] = {0};
+    long long k_count[CS3D_NUM_KERNEL_CLASSES] = {0};
+    int k_cur = -1;
+    cudaEvent_t k_ev0 = nullptr;
+    double *prim_out = nullptr;  // 7 FP64 fields for cs3d_get_field of primitives
+    double *red = nullptr;       // reduction scratch
+    std::vector<void *> allocs;
+};
+
+static cudaEvent_t ev_get(cs3d_handle *h) {
+    if (!h->ev_pool.empty()) {
+        cudaEvent_t e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Drain finished timing events into the per-class totals.
+static int ev_drain(cs3d_handle *h) {
+    for (auto &pe : h->ev_pending) {
+        float ms = 0.f;
+        CS3D_CUDA(cudaEventSynchronize(pe.second.second));
+        CS3D_CUDA(cudaEventElapsedTime(&ms, pe.second.first, pe.second.second));
+        h->k_ms[pe.first] += ms;
+        h->k_count[pe.first] += 1;
+        h->ev_pool.push_back(pe.second.first);
+        h->ev_pool.push_back(pe.second.second);
+    }
+    h->ev_pending.clear();
+    return CS3D_OK;
+}
+
+// Bracket one kernel launch of class cls with events (when timing is on).
+static void tstart(cs3d_handle *h, int cls) {
+    h->launches++;
+    if (!h->timing) return;
+    h->k_cur = cls;
+    h->k_ev0 = ev_get(h);
+    cudaEventRecord(h->k_ev0, h->stream);
+}
+static void tend(cs3d_handle *h) {
+    if (!h->timing || h->k_cur < 0) return;
+    cudaEvent_t e1 = ev_get(h);
+    cudaEventRecord(e1, h->stream);
+    h->ev_pending.push_back({h->k_cur, {h->k_ev0, e1}});
+    h->k_cur = -1;
+    if (h->ev_pending.size() > 4096) ev_drain(h);
+}
+
+static int dalloc(cs3d_handle *h, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(CS3D_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    h->allocs.push_back(*p);
+    e = cudaMemsetAsync(*p, 0, bytes, h->stream);
+    if (e != cudaSuccess) return fail(CS3D_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    return CS3D_OK;
+}
+
+static int face_band_flags(const cs3d_config *c, int *wall, int *spk) {
+    *wall = 0;
+    *spk = 0;
+    for (int f = 0; f < 6; f++) {
+        int k = c->bc_kind[f];
+        if (k == CS3D_ADIABATIC_WALL || k == CS3D_MOVING_ADIABATIC_WALL) *wall |= 1 << f;
+        if (k == CS3D_SPONGE) *spk |= 1 << f;
+    }
+    return 0;
+}
+
+// Wall velocity (U,V,W) of face f (CSolver_AWS.hpp:104-106).
+static void wall_velocity(const cs3d_config *c, int f, double uw[3]) {
+    uw[0] = uw[1] = uw[2] = 0.0;
+    if (c->bc_kind[f] != CS3D_MOVING_ADIABATIC_WALL) return;
+    const double *v = c->wall_vel;
+    switch (f) {
+    case 0: uw[1] = v[0]; uw[2] = v[1]; break;
+    case 1: uw[1] = v[2]; uw[2] = v[3]; break;
+    case 2: uw[0] = v[4]; uw[2] = v[5]; break;
+    case 3: uw[0] = v[6]; uw[2] = v[7]; break;
+    case 4: uw[0] = v[8]; uw[1] = v[9]; break;
+    case 5: uw[0] = v[10]; uw[1] = v[11]; break;
+    }
+}
+
+static int check_config(const cs3d_config *c) {
+    if (!c) return fail(CS3D_ERR_ARG, "null config");
+    int Nd[3] = {c->Nx, c->Ny, c->Nz};
+    double Ld[3] = {c->Lx, c->Ly, c->Lz};
+    for (int d = 0; d < 3; d++) {
+        if (c->bc_type[d] != CS3D_PERIODIC_SOLVE && c->bc_type[d] != CS3D_DIRICHLET_SOLVE)
+            return fail(CS3D_ERR_ARG, "bc_type[%d]=%d is not PERIODIC_SOLVE or DIRICHLET_SOLVE", d, c->bc_type[d]);
+        // the filter's wall closure reaches phi[N-7] (Filter.cpp:77-87); the
+        // periodic filter stencil spans 9 points
+        if (Nd[d] < 8) return fail(CS3D_ERR_SHAPE, "N[%d]=%d: every direction needs at least 8 points", d, Nd[d]);
+        if (Nd[d] > 4096) return fail(CS3D_ERR_SHAPE, "N[%d]=%d exceeds 4096 points per line", d, Nd[d]);
+        if (!(Ld[d] > 0.0)) return fail(CS3D_ERR_ARG, "L[%d] must be positive", d);
+    }
+    for (int f = 0; f < 6; f++)
+        if (c->bc_kind[f] < CS3D_PERIODIC || c->bc_kind[f] > CS3D_INLET)
+            return fail(CS3D_ERR_ARG, "bc_kind[%d]=%d out of range", f, c->bc_kind[f]);
+    if (c->rk != CS3D_RK4 && c->rk != CS3D_TVDRK3) return fail(CS3D_ERR_ARG, "rk=%d", c->rk);
+    if (c->precision != CS3D_FP64 && c->precision != CS3D_FP32_MIXED)
+        return fail(CS3D_ERR_ARG, "precision=%d", c->precision);
+    if (c->filter_step < 1) return fail(CS3D_ERR_ARG, "filter_step must be >= 1");
+    if (!(c->CFL > 0.0) && !(c->dt_fixed > 0.0)) return fail(CS3D_ERR_ARG, "CFL or dt_fixed must be positive");
+    if (c->sponge_mode != CS3D_SPONGE_REFERENCE && c->sponge_mode != CS3D_SPONGE_BANDS)
+        return fail(CS3D_ERR_ARG, "sponge_mode=%d", c->sponge_mode);
+    return CS3D_OK;
+}
+
+// Tile width: the widest power of two (<= 32 lines) whose shared memory fits
+// three blocks per SM.
+static int pick_L(size_t tb, int nbuf, int N, int pitch_plus) {
+    const size_t budget = 72 * 1024;
+    int L = 32;
+    while (L > 1 && sweep_smem_bytes((int)tb, nbuf, L, L + pitch_plus, N) > budget) L /= 2;
+    return L;
+}
+
+// Sponge strength sigma (SpongeBC.hpp:64-150) with sigma starting at zero.
+static void build_sigma(const cs3d_config *c, std::vector<double> &sig, int *any) {
+    const int Nx = c->Nx, Ny = c->Ny, Nz = c->Nz;
+    sig.assign((size_t)Nx * Ny * Nz, 0.0);
+    const double L[3] = {c->Lx, c->Ly, c->Lz};
+    const double dflt[3] = {0.25, 0.125, 0.25};
+    int Nd[3] = {Nx, Ny, Nz};
+    *any = 0;
+    for (int f = 0; f < 6; f++) {
+        int dir = f / 2, hi = f % 2;
+        double band = c->sponge_mode == CS3D_SPONGE_REFERENCE
+                          ? (c->bc_kind[f] == CS3D_SPONGE ? dflt[dir] * L[dir] : 0.0)
+                          : c->sponge_frac[f] * L[dir];
+        if (band <= 0.0) continue;
+        *any = 1;
+        for (int a = 0; a < Nd[dir]; a++) {
+            double xc = (((double)a) / ((double)Nd[dir] - 1.0)) * L[dir], s;
+            if (!hi) { if (!(xc < band)) continue; s = (band - xc) / band; }
+            else { if (!(xc > L[dir] - band)) continue; s = (xc - (L[dir] - band)) / band; }
+            double val = 6.0 * (0.068 * std::pow(s, 2.0) + 0.845 * std::pow(s, 8.0));
+            for (int k = 0; k < Nz; k++)
+                for (int j = 0; j < Ny; j++)
+                    for (int i = 0; i < Nx; i++) {
+                        int id[3] = {i, j, k};
+                        if (id[dir] != a) continue;
+                        size_t ii = (size_t)k * Nx * Ny + (size_t)j * Nx + i;
+                        sig[ii] = std::fmax(val, sig[ii]);
+                    }
+        }
+    }
+}
+
+extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
+    if (!out) return fail(CS3D_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    int rc = check_config(cfg);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(CS3D_ERR_NODEV, "no CUDA device");
+    cs3d_handle *h = new cs3d_handle();
+    h->cfg = *cfg;
+    CS3D_CUDA(cudaGetDevice(&h->dev));
+    CS3D_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->g.Nx = cfg->Nx; h->g.Ny = cfg->Ny; h->g.Nz = cfg->Nz;
+    h->g.npts = (long long)cfg->Nx * cfg->Ny * cfg->Nz;
+    const size_t n = (size_t)h->g.npts;
+    // Domain.hpp:31-45
+    h->dx = (1.0 / ((double)cfg->Nx - 1.0)) * cfg->Lx - 0.0;
+    h->dy = (1.0 / ((double)cfg->Ny - 1.0)) * cfg->Ly - 0.0;
+    h->dz = (1.0 / ((double)cfg->Nz - 1.0)) * cfg->Lz - 0.0;
+    h->gas.gamma = 1.4;
+    h->gas.gm1 = h->gas.gamma - 1;
+    double p_ref = 1.0 / h->gas.gamma;
+    h->gas.R = p_ref / 1.0 / 1.0;
+    double cp = h->gas.R * h->gas.gamma / (h->gas.gamma - 1.0);
+    h->gas.cpPr = cp / 0.7;
+    h->gas.mu_ref = cfg->mu_ref;
+    h->nstages = cfg->rk == CS3D_TVDRK3 ? 3 : 4;
+    h->mixed = cfg->precision == CS3D_FP32_MIXED;
+    h->tb = h->mixed ? 4 : 8;
+    face_band_flags(cfg, &h->wall_faces, &h->sponge_kind_faces);
+    auto fail_free = [&](int code) {
+        cs3d_destroy(h);
+        return code;
+    };
+#define ALLOC(ptr, bytes)                                     \
+    do {                                                      \
+        int r_ = dalloc(h, (void **)&(ptr), (bytes));         \
+        if (r_) return fail_free(r_);                         \
+    } while (0)
+    for (int f = 0; f < 5; f++) {
+        ALLOC(h->q1.f[f], n * 8);
+        ALLOC(h->qk.f[f], n * 8);
+        ALLOC(h->q2.f[f], n * 8);
+        ALLOC(h->prim[f], n * h->tb);
+        ALLOC(h->R[f], n * h->tb);
+        ALLOC(h->ft1[f], n * h->tb);
+        ALLOC(h->ft2[f], n * h->tb);
+    }
+    for (int f = 0; f < 4; f++) {
+        ALLOC(h->dx4[f], n * h->tb);
+        ALLOC(h->dy4[f], n * h->tb);
+    }
+    ALLOC(h->mu, n * h->tb);
+    ALLOC(h->amu, n * h->tb);
+    ALLOC(h->scal, 8 * sizeof(double));
+    ALLOC(h->flag, 4 * sizeof(int));
+    ALLOC(h->red, 1024 * 8 * sizeof(double));
+    // sponge
+    std::vector<double> sig;
+    build_sigma(cfg, sig, &h->sponge);
+    if (h->sponge) {
+        ALLOC(h->sigma, n * 8);
+        for (int f = 0; f < 5; f++) ALLOC(h->savg.f[f], n * 8);
+        CS3D_CUDA(cudaMemcpyAsync(h->sigma, sig.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
+    }
+    if (h->sponge_kind_faces) {
+        for (int f = 0; f < 5; f++) ALLOC(h->backup.f[f], n * 8);
+    }
+    // operators
+    const double dd[3] = {h->dx, h->dy, h->dz};
+    const int Nd[3] = {cfg->Nx, cfg->Ny, cfg->Nz};
+    for (int d = 0; d < 3; d++)
+        for (int k = 1; k <= 3; k++) {
+            HostOp ho = make_op(k, Nd[d], cfg->bc_type[d], dd[d], cfg->alphaF);
+            int r = upload_op<double>(ho, h->op64[d][k - 1], h->stream);
+            if (!r) r = upload_op<float>(ho, h->op32[d][k - 1], h->stream);
+            if (r) return fail_free(r);
+        }
+    for (int d = 0; d < 3; d++) {
+        h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
+        h->Lf[d] = pick_L(h->tb, 5, Nd[d], d == 0 ? 1 : 0);
+    }
+    h->threads = 128;
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    *out = h;
+    return CS3D_OK;
+#undef ALLOC
+}
+
+extern "C" int cs3d_destroy(cs3d_handle *h) {
+    if (!h) return CS3D_OK;
+    DeviceGuard dg(h->dev);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void *p : h->allocs) cudaFree(p);
+    for (int d = 0; d < 3; d++)
+        for (int k = 0; k < 3; k++) {
+            if (h->op64[d][k].mem) cudaFree(h->op64[d][k].mem);
+            if (h->op32[d][k].mem) cudaFree(h->op32[d][k].mem);
+        }
+    if (h->dq[0]) for (int f = 0; f < 5; f++) cudaFree(h->dq[f]);
+    if (h->diag[0]) for (int f = 0; f < 3; f++) cudaFree(h->diag[f]);
+    if (h->prim_out) cudaFree(h->prim_out);
+    for (auto &pe : h->ev_pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------
+static int launch_cfl_reduce(cs3d_handle *h) {
+    CS3D_CUDA(cudaMemsetAsync(h->scal + 2, 0, sizeof(double), h->stream));
+    CflArgs a{};
+    a.g = h->g;
+    a.gas = h->gas;
+    a.q = h->q1;
+    a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
+    a.max_out = h->scal + 2;
+    a.nan_flag = h->flag;
+    tstart(h, CS3D_K_CFL);
+    CS3D_CUDA(launch_cfl(a, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, const double *p0, const double *U0,
+                                           const double *V0, const double *W0) {
+    if (!h || !rho0 || !p0 || !U0 || !V0 || !W0) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    double *tmp = nullptr;
+    CS3D_CUDA(cudaMalloc(&tmp, n * 8 * 6));
+    double *d_rho = tmp, *d_p = tmp + n, *d_U = tmp + 2 * n, *d_V = tmp + 3 * n, *d_W = tmp + 4 * n, *d_T = tmp + 5 * n;
+    CS3D_CUDA(cudaMemcpyAsync(d_rho, rho0, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(d_p, p0, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(d_U, U0, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(d_V, V0, n * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(d_W, W0, n * 8, cudaMemcpyHostToDevice, h->stream));
+    IcArgs a{};
+    a.g = h->g;
+    a.gas = h->gas;
+    a.rho0 = d_rho; a.p0 = d_p; a.U0 = d_U; a.V0 = d_V; a.W0 = d_W; a.T0 = d_T;
+    a.q1 = h->q1;
+    CS3D_CUDA(launch_ic(a, h->stream));
+    h->launches++;
+    if (h->wall_faces) {
+        for (int pass = 0; pass < 2; pass++) {
+            int kind = pass == 0 ? CS3D_ADIABATIC_WALL : CS3D_MOVING_ADIABATIC_WALL;
+            for (int f = 0; f < 6; f++) {
+                if (h->cfg.bc_kind[f] != kind) continue;
+                a.face = f;
+                wall_velocity(&h->cfg, f, a.uw);
+                CS3D_CUDA(launch_ic_wall(a, h->stream));
+                h->launches++;
+            }
+        }
+        CS3D_CUDA(launch_ic_wall_eos(a, h->stream));
+        h->launches++;
+    }
+    if (h->sponge)
+        for (int f = 0; f < 5; f++)
+            CS3D_CUDA(cudaMemcpyAsync(h->savg.f[f], h->q1.f[f], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    // reference values of the mixed filter: the field means of the initial state
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->mixed) {
+        std::vector<double> hb(n);
+        for (int f = 0; f < 5; f++) {
+            CS3D_CUDA(cudaMemcpy(hb.data(), h->q1.f[f], n * 8, cudaMemcpyDeviceToHost));
+            long double s = 0;
+            for (size_t i = 0; i < n; i++) s += hb[i];
+            h->fref[f] = (double)(s / (long double)n);
+        }
+    }
+    CS3D_CUDA(cudaFree(tmp));
+    h->timeStep = 0;
+    h->filterTimeStep = 0;
+    h->backup_valid = 0;
+    CS3D_CUDA(cudaMemsetAsync(h->scal, 0, 8 * sizeof(double), h->stream));
+    CS3D_CUDA(cudaMemsetAsync(h->flag, 0, 4 * sizeof(int), h->stream));
+    int rc = launch_cfl_reduce(h);
+    if (rc) return rc;
+    h->ic_done = 1;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_pre_step(cs3d_handle *h) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    DeviceGuard dg(h->dev);
+    DtArgs a{};
+    a.max_in = h->scal + 2;
+    a.dt = h->scal + 0;
+    a.time = h->scal + 1;
+    a.CFL = h->cfg.CFL;
+    a.dt_fixed = h->cfg.dt_fixed;
+    a.first = h->timeStep == 0;
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_finalize_dt(a, h->stream));
+    tend(h);
+    h->timeStep++;
+    return CS3D_OK;
+}
+
+template <typename T>
+static int run_stage(cs3d_handle *h, int st, int last) {
+    const Q5 qs = st == 1 ? h->q1 : h->qk;
+    const int use_backup = st == 1 && h->backup_valid;
+    // walls before the derivatives
+    if (h->wall_faces) {
+        BCArgs b{};
+        b.g = h->g;
+        b.gas = h->gas;
+        b.q = qs;
+        b.backup = h->backup;
+        b.use_backup = use_backup;
+        b.wall_faces = h->wall_faces;
+        b.sponge_faces = h->sponge_kind_faces;
+        for (int pass = 0; pass < 2; pass++) {
+            int kind = pass == 0 ? CS3D_ADIABATIC_WALL : CS3D_MOVING_ADIABATIC_WALL;
+            for (int f = 0; f < 6; f++) {
+                if (h->cfg.bc_kind[f] != kind) continue;
+                b.face = f;
+                wall_velocity(&h->cfg, f, b.uw);
+                tstart(h, CS3D_K_BOUNDARY);
+                CS3D_CUDA(launch_wall_pre(b, h->stream));
+                tend(h);
+            }
+        }
+    }
+    SweepArgs<T> a{};
+    a.g = h->g;
+    a.threads = h->threads;
+    a.gas = h->gas;
+    a.q = qs;
+    a.backup = h->backup;
+    a.use_backup = use_backup;
+    a.wall_faces = h->wall_faces;
+    a.sponge_faces = h->sponge_kind_faces;
+    a.sponge_kind_faces = h->sponge_kind_faces;
+    for (int f = 0; f < 5; f++) {
+        a.prim[f] = (T *)h->prim[f];
+        a.R[f] = (T *)h->R[f];
+        a.dq_out[f] = h->store_dq ? h->dq[f] : nullptr;
+    }
+    a.mu = (T *)h->mu;
+    a.amu = (T *)h->amu;
+    for (int f = 0; f < 4; f++) {
+        a.dx[f] = (T *)h->dx4[f];
+        a.dy[f] = (T *)h->dy4[f];
+    }
+    for (int f = 0; f < 3; f++) a.diag[f] = h->store_diag ? (T *)h->diag[f] : nullptr;
+    if (!h->store_diag) a.diag[0] = nullptr;
+    a.dt = h->scal;
+    a.rk = h->cfg.rk == CS3D_TVDRK3 ? 1 : 0;
+    a.rk_step = st;
+    a.q1 = h->q1;
+    a.q2 = h->q2;
+    a.qk = h->qk;
+    a.sponge = h->sponge;
+    a.sigma = h->sigma;
+    a.savg = h->savg;
+    for (int d = 0; d < 3; d++) {
+        a.L = h->L[d];
+        a.P = h->L[d] + (d == 0 ? 1 : 0);
+        if (sizeof(T) == 8) {
+            a.d1 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][0].op);
+            a.d2 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][1].op);
+        } else {
+            a.d1 = *reinterpret_cast<const LineOp<T> *>(&h->op32[d][0].op);
+            a.d2 = *reinterpret_cast<const LineOp<T> *>(&h->op32[d][1].op);
+        }
+        tstart(h, CS3D_K_SWEEP_X + d);
+        CS3D_CUDA(launch_sweep<T>(d, a, h->stream));
+        tend(h);
+    }
+    if (last) {
+        if (h->timeStep % h->cfg.filter_step == 0) {
+            // filterConservedData round robin (CSolver_AWS.cpp:1690-1863)
+            h->filterTimeStep++;
+            int order[3];
+            int m3 = h->filterTimeStep % 3;
+            if (m3 == 1) { order[0] = 0; order[1] = 1; order[2] = 2; }
+            else if (m3 == 2) { order[0] = 1; order[1] = 2; order[2] = 0; }
+            else { order[0] = 2; order[1] = 0; order[2] = 1; }
+            for (int pass = 0; pass < 3; pass++) {
+                int d = order[pass];
+                FilterArgs<T> fa{};
+                fa.g = h->g;
+                fa.L = h->Lf[d];
+                fa.P = h->Lf[d] + (d == 0 ? 1 : 0);
+                fa.threads = h->threads;
+                if (sizeof(T) == 8) fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][2].op);
+                else fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op32[d][2].op);
+                void **src = pass == 1 ? h->ft1 : h->ft2;
+                void **dst = pass == 0 ? h->ft1 : h->ft2;
+                for (int f = 0; f < 5; f++) {
+                    fa.ref[f] = h->mixed ? h->fref[f] : 0.0;
+                    fa.src64.f[f] = pass == 0 ? h->q2.f[f] : nullptr;
+                    fa.src32[f] = pass == 0 ? nullptr : (T *)src[f];
+                    fa.dst64.f[f] = pass == 2 ? h->q1.f[f] : nullptr;
+                    fa.dst32[f] = pass == 2 ? nullptr : (T *)dst[f];
+                    fa.delta_from.f[f] = (pass == 2 && h->mixed) ? h->q2.f[f] : nullptr;
+                }
+                tstart(h, CS3D_K_FILTER);
+                CS3D_CUDA(launch_filter<T>(d, fa, h->stream));
+                tend(h);
+            }
+        } else {
+            std::swap(h->q1, h->q2);
+        }
+        int rc = launch_cfl_reduce(h);
+        if (rc) return rc;
+    }
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_sub_step(cs3d_handle *h, int rk_step, int rk_last) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    if (h->timeStep < 1) return fail(CS3D_ERR_STATE, "cs3d_pre_step must precede the first sub-step");
+    if (rk_step < 1 || rk_step > h->nstages) return fail(CS3D_ERR_ARG, "rk_step=%d", rk_step);
+    DeviceGuard dg(h->dev);
+    return h->mixed ? run_stage<float>(h, rk_step, rk_last) : run_stage<double>(h, rk_step, rk_last);
+}
+
+extern "C" int cs3d_post_step(cs3d_handle *h) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (!h->sponge) return CS3D_OK;
+    DeviceGuard dg(h->dev);
+    SpongeArgs a{};
+    a.g = h->g;
+    a.dt = h->scal;
+    a.avgT = 15.0;         // SpongeBC.hpp:56-58
+    a.epsP = 0.005;
+    a.spongeP = 1.0 / h->gas.gamma;
+    a.gm1 = h->gas.gamma - 1.0;
+    a.q1 = h->q1;
+    a.savg = h->savg;
+    a.backup = h->backup;
+    a.sponge_kind_faces = h->sponge_kind_faces;
+    tstart(h, CS3D_K_SPONGE);
+    CS3D_CUDA(launch_sponge_update(a, h->stream));
+    tend(h);
+    if (h->sponge_kind_faces) h->backup_valid = 1;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_step(cs3d_handle *h) {
+    int rc = cs3d_pre_step(h);
+    if (rc) return rc;
+    for (int s = 1; s <= h->nstages; s++) {
+        rc = cs3d_sub_step(h, s, s == h->nstages);
+        if (rc) return rc;
+    }
+    return cs3d_post_step(h);
+}
+
+extern "C" int cs3d_run(cs3d_handle *h, int n) {
+    for (int i = 0; i < n; i++) {
+        int rc = cs3d_step(h);
+        if (rc) return rc;
+    }
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_sync(cs3d_handle *h) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    DeviceGuard dg(h->dev);
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    CflArgs a{};
+    a.g = h->g;
+    a.q = h->q1;
+    a.nan_flag = h->flag;
+    CS3D_CUDA(launch_nan_scan(a, h->stream));
+    h->launches++;
+    int flag = 0;
+    CS3D_CUDA(cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    if (flag) {
+        CS3D_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+        return fail(CS3D_ERR_NAN, "a non-finite value reached the conserved state");
+    }
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// field access
+// ---------------------------------------------------------------------
+static int field_ptr(cs3d_handle *h, int field, double **p) {
+    *p = nullptr;
+    if (field >= CS3D_F_RHO1 && field < CS3D_F_RHO1 + 5) *p = h->q1.f[field - CS3D_F_RHO1];
+    else if (field >= CS3D_F_RHOK && field < CS3D_F_RHOK + 5) *p = h->qk.f[field - CS3D_F_RHOK];
+    else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) *p = h->q2.f[field - CS3D_F_RHO2];
+    else if (field >= CS3D_F_RHOK2 && field < CS3D_F_RHOK2 + 5) {
+        if (!h->store_dq) return fail(CS3D_ERR_STATE, "increments are kept only with CS3D_OPT_STORE_INCREMENTS");
+        *p = h->dq[field - CS3D_F_RHOK2];
+    } else if (field >= CS3D_F_U && field < CS3D_F_U + 7) {
+        if (!h->prim_out) CS3D_CUDA(cudaMalloc(&h->prim_out, (size_t)h->g.npts * 8 * 7));
+        PrimArgs a{};
+        a.g = h->g;
+        a.gas = h->gas;
+        a.q = h->q1;
+        for (int f = 0; f < 7; f++) a.out[f] = h->prim_out + (size_t)f * h->g.npts;
+        CS3D_CUDA(launch_primitives(a, h->stream));
+        h->launches++;
+        *p = h->prim_out + (size_t)(field - CS3D_F_U) * h->g.npts;
+    } else if (field >= CS3D_F_SPONGE_AVG && field < CS3D_F_SPONGE_AVG + 5) {
+        if (!h->sponge) return fail(CS3D_ERR_STATE, "no sponge in this configuration");
+        *p = h->savg.f[field - CS3D_F_SPONGE_AVG];
+    } else if (field == CS3D_F_SIGMA) {
+        if (!h->sponge) return fail(CS3D_ERR_STATE, "no sponge in this configuration");
+        *p = h->sigma;
+    } else {
+        return fail(CS3D_ERR_ARG, "field index %d out of range", field);
+    }
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_get_field(cs3d_handle *h, int field, double *host_out) {
+    if (!h || !host_out) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    double *p;
+    int rc = field_ptr(h, field, &p);
+    if (rc) return rc;
+    CS3D_CUDA(cudaMemcpyAsync(host_out, p, (size_t)h->g.npts * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_set_field(cs3d_handle *h, int field, const double *host_in) {
+    if (!h || !host_in) return fail(CS3D_ERR_ARG, "null argument");
+    if (field >= CS3D_F_U && field < CS3D_F_U + 7)
+        return fail(CS3D_ERR_ARG, "primitive fields are derived from the conserved state and cannot be set");
+    DeviceGuard dg(h->dev);
+    double *p;
+    int rc = field_ptr(h, field, &p);
+    if (rc) return rc;
+    CS3D_CUDA(cudaMemcpyAsync(p, host_in, (size_t)h->g.npts * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_field_ptr(cs3d_handle *h, int field, double **dev_ptr) {
+    if (!h || !dev_ptr) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    return field_ptr(h, field, dev_ptr);
+}
+
+extern "C" int cs3d_get_scalars(cs3d_handle *h, double *dt, double *time, int *time_step) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    DeviceGuard dg(h->dev);
+    double s[2];
+    CS3D_CUDA(cudaMemcpyAsync(s, h->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    if (dt) *dt = s[0];
+    if (time) *time = s[1];
+    if (time_step) *time_step = h->timeStep;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_get_stream(cs3d_handle *h, void **stream) {
+    if (!h || !stream) return fail(CS3D_ERR_ARG, "null argument");
+    *stream = (void *)h->stream;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_launch_count(cs3d_handle *h, long long *count) {
+    if (!h || !count) return fail(CS3D_ERR_ARG, "null argument");
+    *count = h->launches;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_set_option(cs3d_handle *h, int option, int value) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    if (option == CS3D_OPT_STORE_INCREMENTS) {
+        if (value && !h->dq[0])
+            for (int f = 0; f < 5; f++) {
+                CS3D_CUDA(cudaMalloc(&h->dq[f], n * 8));
+                CS3D_CUDA(cudaMemsetAsync(h->dq[f], 0, n * 8, h->stream));
+            }
+        h->store_dq = value != 0;
+    } else if (option == CS3D_OPT_STORE_DIAGNOSTICS) {
+        if (value && !h->diag[0])
+            for (int f = 0; f < 3; f++) {
+                CS3D_CUDA(cudaMalloc(&h->diag[f], n * h->tb));
+                CS3D_CUDA(cudaMemsetAsync(h->diag[f], 0, n * h->tb, h->stream));
+            }
+        h->store_diag = value != 0;
+    } else if (option == CS3D_OPT_KERNEL_TIMING) {
+        h->timing = value != 0;
+    } else {
+        return fail(CS3D_ERR_ARG, "unknown option %d", option);
+    }
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_kernel_times(cs3d_handle *h, double *ms, long long *count, int n, int reset) {
+    if (!h || (!ms && !count)) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    int rc = ev_drain(h);
+    if (rc) return rc;
+    for (int i = 0; i < n && i < CS3D_NUM_KERNEL_CLASSES; i++) {
+        if (ms) ms[i] = h->k_ms[i];
+        if (count) count[i] = h->k_count[i];
+    }
+    if (reset)
+        for (int i = 0; i < CS3D_NUM_KERNEL_CLASSES; i++) { h->k_ms[i] = 0; h->k_count[i] = 0; }
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// single operators
+// ---------------------------------------------------------------------
+static int line_op(cs3d_handle *h, int kind, int dir, const double *in, double *out) {
+    if (!h || !in || !out) return fail(CS3D_ERR_ARG, "null argument");
+    if (dir < 0 || dir > 2) return fail(CS3D_ERR_ARG, "dir=%d", dir);
+    if (in == out) return fail(CS3D_ERR_ARG, "in and out must not overlap");
+    DeviceGuard dg(h->dev);
+    LineOpArgs a{};
+    a.op = h->op64[dir][kind - 1].op;
+    const int N = a.op.N;
+    a.nlines = h->g.npts / N;
+    a.L = 32;
+    while (a.L > 1 && sweep_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
+    a.P = a.L + 1;
+    a.threads = 128;
+    a.in = in;
+    a.out = out;
+    CS3D_CUDA(launch_line_op(a, h->stream));
+    h->launches++;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_deriv1(cs3d_handle *h, int dir, const double *in_dev, double *out_dev) {
+    return line_op(h, 1, dir, in_dev, out_dev);
+}
+extern "C" int cs3d_deriv2(cs3d_handle *h, int dir, const double *in_dev, double *out_dev) {
+    return line_op(h, 2, dir, in_dev, out_dev);
+}
+extern "C" int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev) {
+    return line_op(h, 3, dir, in_dev, out_dev);
+}
+
+// ---------------------------------------------------------------------
+// Taylor-Green diagnostics
+// ---------------------------------------------------------------------
+template <typename T>
+static int tgv_launch(cs3d_handle *h, int blocks) {
+    TgvArgs<T> a{};
+    a.g = h->g;
+    a.gas = h->gas;
+    a.q = h->q1;
+    for (int f = 0; f < 3; f++) {
+        a.dx[f] = (const T *)h->dx4[f];
+        a.dy[f] = (const T *)h->dy4[f];
+        a.dz[f] = (const T *)h->diag[f];
+    }
+    a.out = h->red;
+    CS3D_CUDA(launch_tgv<T>(a, blocks, h->stream));
+    h->launches++;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_tgv_quantities(cs3d_handle *h, double out[7]) {
+    if (!h || !out) return fail(CS3D_ERR_ARG, "null argument");
+    if (!h->store_diag || h->timeStep < 1)
+        return fail(CS3D_ERR_STATE, "run a step with CS3D_OPT_STORE_DIAGNOSTICS on first");
+    DeviceGuard dg(h->dev);
+    const int blocks = 1024;
+    int rc = h->mixed ? tgv_launch<float>(h, blocks) : tgv_launch<double>(h, blocks);
+    if (rc) return rc;
+    std::vector<double> part((size_t)blocks * 6);
+    double t[2];
+    CS3D_CUDA(cudaMemcpyAsync(part.data(), h->red, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(t, h->scal, 2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < blocks; b++)
+        for (int i = 0; i < 6; i++) s[i] += part[(size_t)b * 6 + i];
+    out[0] = t[1];
+    out[1] = s[3];
+    out[2] = s[2];
+    out[3] = s[0];
+    out[4] = s[1];
+    out[5] = s[5];
+    out[6] = std::sqrt(s[4]);
+    return CS3D_OK;
+}

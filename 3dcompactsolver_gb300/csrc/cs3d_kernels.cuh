@@ -1,0 +1,149 @@
+// cs3d_kernels.cuh -- kernel argument blocks and launch functions.
+#pragma once
+#include "cs3d_dev.cuh"
+
+namespace cs3d {
+
+// Ideal-gas constants (IdealGas.hpp:36-46).
+struct GasParams {
+    double gamma;   // 1.4
+    double gm1;     // gamma - 1
+    double R;       // p_ref / rho_ref / T_ref
+    double cpPr;    // cp / Pr
+    double mu_ref;
+};
+
+template <typename T>
+struct SweepArgs {
+    Geom g;
+    int L;          // lines per tile
+    int P;          // shared-memory pitch between positions of a line
+    int threads;    // threads per block
+    LineOp<T> d1, d2;
+    GasParams gas;
+    Q5 q;           // stage input q* (FP64)
+    Q5 backup;      // q1 before the last sponge overwrite (SPONGE faces)
+    int use_backup; // stage 1 after a sponge overwrite
+    int wall_faces;         // bit per face: wall (adiabatic or moving)
+    int sponge_faces;       // bit per face: SPONGE kind (for the backup rule)
+    int sponge_kind_faces;  // bit per face: SPONGE kind (increments zeroed)
+    T *prim[5];     // U V W p T of q*
+    T *mu, *amu;    // mu(T), dmu/dT
+    T *dx[4];       // Ux Vx Wx Tx
+    T *dy[4];       // Uy Vy Wy Ty
+    T *R[5];        // right-hand-side accumulators
+    T *diag[3];     // Uz Vz Wz of the stage (optional)
+    // z sweep only
+    const double *dt;
+    int rk, rk_step;
+    Q5 q1, q2, qk;
+    int sponge;
+    const double *sigma;
+    Q5 savg;
+    double *dq_out[5];  // increments dq (optional)
+};
+
+template <typename T>
+struct FilterArgs {
+    Geom g;
+    int L, P, threads;
+    LineOp<T> op;
+    Q5 src64;          // FP64 source (or null pointers)
+    T *src32[5];       // work-precision source
+    Q5 dst64;          // FP64 destination (or null pointers)
+    T *dst32[5];       // work-precision destination
+    Q5 delta_from;     // mixed last pass: q1 = q2 + (filtered - unfiltered)
+    double ref[5];     // per-field reference value subtracted on entry
+};
+
+struct LineOpArgs {
+    int L, P, threads;
+    long long nlines;
+    LineOp<double> op;
+    const double *in;
+    double *out;
+};
+
+struct BCArgs {
+    Geom g;
+    int face;
+    double uw[3];
+    GasParams gas;
+    Q5 q;
+    Q5 backup;
+    int use_backup;
+    int wall_faces, sponge_faces;
+};
+
+struct CflArgs {
+    Geom g;
+    GasParams gas;
+    Q5 q;
+    double dx, dy, dz;
+    double *max_out;
+    int *nan_flag;
+};
+
+struct DtArgs {
+    const double *max_in;
+    double *dt, *time;
+    double CFL, dt_fixed;
+    int first;
+};
+
+struct SpongeArgs {
+    Geom g;
+    const double *dt;
+    double avgT, epsP, spongeP, gm1;
+    Q5 q1, savg, backup;
+    int sponge_kind_faces;
+};
+
+struct IcArgs {
+    Geom g;
+    GasParams gas;
+    const double *rho0, *p0;
+    double *U0, *V0, *W0, *T0;
+    Q5 q1;
+    int face;
+    double uw[3];
+};
+
+struct PrimArgs {
+    Geom g;
+    GasParams gas;
+    Q5 q;
+    double *out[7];
+};
+
+template <typename T>
+struct TgvArgs {
+    Geom g;
+    GasParams gas;
+    Q5 q;
+    const T *dx[3], *dy[3], *dz[3];
+    double *out;  // [blocks][6]
+};
+
+template <typename T>
+cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s);
+template <typename T>
+cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s);
+cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s);
+cudaError_t launch_wall_pre(const BCArgs &a, cudaStream_t s);
+cudaError_t launch_cfl(const CflArgs &a, cudaStream_t s);
+cudaError_t launch_nan_scan(const CflArgs &a, cudaStream_t s);
+cudaError_t launch_finalize_dt(const DtArgs &a, cudaStream_t s);
+cudaError_t launch_sponge_update(const SpongeArgs &a, cudaStream_t s);
+cudaError_t launch_ic(const IcArgs &a, cudaStream_t s);
+cudaError_t launch_ic_wall(const IcArgs &a, cudaStream_t s);
+cudaError_t launch_ic_wall_eos(const IcArgs &a, cudaStream_t s);
+cudaError_t launch_primitives(const PrimArgs &a, cudaStream_t s);
+
+size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N);
+int sweep_nbuf(int dir);
+int sweep_ntask(int dir);
+
+}  // namespace cs3d

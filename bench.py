@@ -1,0 +1,429 @@
+"""Benchmark of the GB300 stage path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload tgv128|tgv64|hit256|shear] [--precision mixed|fp64]
+
+Prints ONE JSON line on rank 0.  The metric is the benchmark's: million grid
+points advanced per second per Runge-Kutta stage ("Mpts/s per RK stage"),
+i.e. npts * stages * steps / seconds.  A "step" is one full time step of the
+solver (4 RK4 stages or 3 TVD-RK3 stages, the filter and the CFL reduction).
+
+Our arm times the chosen form (FP32-mixed, unless --precision fp64) with
+device-resident inputs (`value`), the plain FP64 form beside it, and the same
+metric end to end through the public API with pinned host buffers (`e2e`).
+The reference arm (--impl reference) times the CPU restatement of the
+reference algorithm (oracle/, built with the reference's own compiler flags)
+on all host cores.  Multi-GPU runs are independent replicas (the path does
+not shard without an all-to-all exchange); value sums all ranks.
+"""
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpts/s per RK stage: FP32-mixed vs FP64 on one GB300 at stated KE error"
+UNIT = "Mpts/s per RK stage"
+
+# Algorithmic bytes per grid point of each kernel launch, for the roofline.
+# Counted from the arrays each kernel must read and write once (state FP64;
+# work arrays 4 bytes in the mixed form, 8 in the plain form); see the
+# kernel byte model in the design doc.
+def kernel_bytes_per_point(kernel, wb, rk_stages):
+    if kernel == "sweep_x":
+        return 40 + wb * (5 + 2 + 4 + 5)              # q* in; prims, mu, mu', 4 derivs, 5 RHS out
+    if kernel == "sweep_y":
+        return 32 + wb * (5 + 2 + 1 + 5) + wb * (4 + 5)  # q*(4), prims, Ux Vx, mu, RHS in; 4 derivs, RHS out
+    if kernel == "sweep_z":
+        common = 40 + wb * (5 + 4 + 4 + 2 + 5)        # q*, prims, x/y derivs, mu mu', RHS
+        if rk_stages == 4:   # RK4: st1 writes q2,qk; st2-3 read q1,q2 write q2,qk; st4 reads q1,q2 writes q2
+            per = [common + 80, common + 80 + 80, common + 80 + 80, common + 80 + 40]
+        else:                # TVD-RK3: st1 writes qk; st2 reads q1 writes qk; st3 reads q1 writes q2
+            per = [common + 40, common + 40 + 40, common + 40 + 40]
+        return sum(per) / len(per)
+    if kernel == "filter":
+        if wb == 8:
+            return 80.0                                # 5 fields in, 5 out, FP64
+        return (40 + 20 + 20 + 20 + 20 + 40 + 40) / 3.0  # mixed: q2 in, FP32 passes, q2 + q1 last
+    if kernel == "cfl":
+        return 40.0
+    return 0.0
+
+
+def _pkg():
+    return importlib.import_module("3dcompactsolver_gb300")
+
+
+def _cases():
+    return importlib.import_module("3dcompactsolver_gb300.cases")
+
+
+def make_workload(name, precision):
+    c = _cases()
+    abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    prec = abi.FP32_MIXED if precision == "mixed" else abi.FP64
+    if name == "tgv128":
+        cfg, ic = c.tgv(128, precision=prec)
+        desc = "Taylor-Green vortex 128^3, RK4, CFL 0.5, alphaF 0.49, filter every step, Re 1600, Mach 0.1"
+    elif name == "tgv64":
+        cfg, ic = c.tgv(64, precision=prec)
+        desc = "Taylor-Green vortex 64^3, RK4, CFL 0.5, alphaF 0.49, filter every step, Re 1600, Mach 0.1"
+    elif name == "hit256":
+        cfg, ic = c.hit(256, precision=prec)
+        desc = "decaying isotropic turbulence 256^3, RK4, Mt 0.3, E(k)~(k/8)^4 exp(-2(k/8)^2), seed 0"
+    elif name == "shear":
+        cfg, ic = c.shear_layer(256, 128, 42, precision=prec)
+        desc = "temporal shear layer 256x128x42, TVD-RK3, y walls + 15% sponge, Mach 0.3, seed 0"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return cfg, ic, desc
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken every 20 ms; only samples whose
+    timestamps fall inside the timed region are kept."""
+    QUERY = ("timestamp,index,uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_uuid):
+        self.uuid = device_uuid
+        self.proc = None
+        self.path = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits", "-lms", "20"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def mark(self, which):
+        from datetime import datetime
+        if which == 0:
+            self.t0 = datetime.now()
+        else:
+            self.t1 = datetime.now()
+
+    def stop(self):
+        from datetime import datetime, timedelta
+        if self.proc is None:
+            return None
+        time.sleep(0.1)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 11:
+                    continue
+                if self.uuid and parts[2] != self.uuid:
+                    continue
+                try:
+                    ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                    rows.append((ts, float(parts[3]), float(parts[4]), parts[7:11]))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        lo = self.t0 - timedelta(milliseconds=25) if self.t0 else rows[0][0]
+        hi = self.t1 + timedelta(milliseconds=25) if self.t1 else rows[-1][0]
+        inside = [r for r in rows if lo <= r[0] <= hi] or rows[-3:]
+        reasons = set()
+        for r in inside:
+            for n, v in zip(names, r[3]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": inside[-1][2],
+                "reasons": sorted(reasons), "samples": len(inside)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(value, ws):
+    """Barrier, then the maximum of value over ranks (value on every rank)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def kinetic_energy(q):
+    rho = q[0]
+    return float(0.5 * np.sum((q[1] ** 2 + q[2] ** 2 + q[3] ** 2) / rho))
+
+
+def time_steps(solver, steps, torch):
+    """Device time of `steps` time steps on the solver's stream (ms)."""
+    stream = torch.cuda.ExternalStream(solver.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    solver.run(steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def cpu_baseline(workload, seconds=12.0):
+    """The oracle restatement (reference flags, OpenMP on all cores) on a
+    bounded sample of the workload: one warm-up step, then whole steps until
+    `seconds` of CPU time have passed (at least one)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle_fast.so")):
+        oracle.build()
+    cfg, ic, desc = make_workload(workload, "fp64")
+    p = oracle.OraclePort(cfg, "fast")
+    p.set_initial_conditions(*ic)
+    p.step()
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        p.step()
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    stages = 3 if cfg.rk == 1 else 4
+    val = cfg.npts * stages * n / el / 1e6
+    cores = oracle.port_lib("fast").or_num_threads()
+    return {"value": round(val, 3), "unit": UNIT, "cores": int(cores), "kind": "port",
+            "sample": f"{desc}; 1 warm-up + {n} timed step(s) of the oracle restatement "
+                      f"(oracle/cs3d_oracle.c, -O3 -ffast-math -funroll-loops -fopenmp)"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if not os.path.exists(os.path.join(ROOT, "oracle", "liboracle_fast.so")):
+        oracle.build()
+    cfg, ic, desc = make_workload(args.workload, "fp64")
+    p = oracle.OraclePort(cfg, "fast")
+    p.set_initial_conditions(*ic)
+    for _ in range(min(args.warmup, 1)):
+        p.step()
+    budget = 150.0
+    n = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        p.step()
+        n += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    stages = 3 if cfg.rk == 1 else 4
+    val = cfg.npts * stages * n / el / 1e6
+    cores = oracle.port_lib("fast").or_num_threads()
+    cb = {"value": round(val, 3), "unit": UNIT, "cores": int(cores), "kind": "port",
+          "sample": f"{desc}; {min(args.warmup, 1)} warm-up + {n} timed step(s), FP64, OpenMP"}
+    line = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": round(1e3 * el / max(n, 1), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc, "npts": cfg.npts},
+            "cpu_baseline": cb,
+            "e2e": {"value": round(val, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = _dist()
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    pkg = _pkg()
+    importlib.import_module("3dcompactsolver_gb300.build").build()
+    cfg, ic, desc = make_workload(args.workload, args.precision)
+    stages = 3 if cfg.rk == 1 else 4
+    npts = cfg.npts
+    wb = 4 if args.precision == "mixed" else 8
+
+    # the chosen form
+    s = pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.run(args.warmup)
+    s.sync()
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        uuid = None
+    sampler = ClockSampler(uuid)
+    sampler.start()
+    _barrier(ws)
+    n0 = s.launch_count()
+    sampler.mark(0)
+    ms = time_steps(s, args.steps, torch)
+    sampler.mark(1)
+    launches = s.launch_count() - n0
+    clocks = sampler.stop()
+    ms = _barrier_max(ms, ws)
+    value = ws * npts * stages * args.steps / (ms / 1e3) / 1e6
+
+    # per-kernel device times (events on the library's stream) for the roofline
+    s.set_option(pkg.OPT_KERNEL_TIMING, 1)
+    s.kernel_times(reset=True)
+    s.run(args.steps)
+    kt = s.kernel_times(reset=True)
+    s.set_option(pkg.OPT_KERNEL_TIMING, 0)
+    s.sync()
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    dom = max((k for k in kt if kt[k][1] > 0), key=lambda k: kt[k][0])
+    avg_ms = kt[dom][0] / kt[dom][1]
+    bpp = kernel_bytes_per_point(dom, wb, stages)
+    achieved = bpp * npts / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "dram_bytes_per_point.json")
+    if os.path.exists(tr_path):
+        tr = json.load(open(tr_path))
+        key = f"{args.precision}:{dom}"
+        if key in tr:
+            traffic = round(tr[key] * npts)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
+                "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+                "peak_source": peak_src, "bytes_per_point": bpp, "avg_launch_ms": round(avg_ms, 4),
+                "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+    # stage-level fraction against the byte model of the whole stage
+    stage_bytes = sum(kernel_bytes_per_point(k, wb, stages) * (kt[k][1] / args.steps)
+                      for k in ("sweep_x", "sweep_y", "sweep_z", "filter", "cfl")) * npts
+    roofline["stage_frac"] = round(stage_bytes / (ms / args.steps / 1e3) / 1e9 / hbm_peak / ws, 4)
+
+    # end to end through the public API: pinned host state in, one step, state out
+    q_host = [torch.empty(cfg.shape, dtype=torch.float64).pin_memory() for _ in range(5)]
+    for f in range(5):
+        q_host[f].numpy()[...] = s.get(f)
+    lib = pkg.lib()
+    ptrs = [q.numpy().ctypes.data_as(pkg._DP) for q in q_host]
+    torch.cuda.synchronize()
+    _barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for f in range(5):
+            pkg.check(lib.cs3d_set_field(s.h, f, ptrs[f]))
+        pkg.check(lib.cs3d_step(s.h))
+        for f in range(5):
+            pkg.check(lib.cs3d_get_field(s.h, f, ptrs[f]))
+    e2e_s = _barrier_max(time.perf_counter() - t0, ws)
+    e2e_val = ws * npts * stages * args.steps / e2e_s / 1e6
+
+    # the other form on the same workload and the KE error of the mixed form
+    other = {}
+    if not args.no_fp64:
+        other_prec = "fp64" if args.precision == "mixed" else "mixed"
+        cfg2, ic2, _ = make_workload(args.workload, other_prec)
+        s2 = pkg.Solver(cfg2)
+        s2.set_initial_conditions(*ic2)
+        s2.run(args.warmup)
+        s2.sync()
+        ms2 = _barrier_max(time_steps(s2, args.steps, torch), ws)
+        # both forms have now advanced warmup + steps steps; the chosen form has
+        # run 2*steps more (timing pass and e2e): compare at equal step counts
+        s3 = pkg.Solver(cfg)
+        s3.set_initial_conditions(*ic)
+        s3.run(args.warmup + args.steps)
+        s3.sync()
+        ke_m = kinetic_energy(s3.conserved() if args.precision == "mixed" else s2.conserved())
+        ke_d = kinetic_energy(s2.conserved() if args.precision == "mixed" else s3.conserved())
+        v2 = ws * npts * stages * args.steps / (ms2 / 1e3) / 1e6
+        other = {"other_form": {"precision": other_prec, "value": round(v2, 3), "unit": UNIT,
+                                "ms_per_step": round(ms2 / args.steps, 4)},
+                 "mixed_over_fp64": round((value / v2) if args.precision == "mixed" else (v2 / value), 3),
+                 "ke_rel_err_vs_fp64": float(abs(ke_m - ke_d) / abs(ke_d)),
+                 "ke_steps": args.warmup + args.steps}
+        s2.close()
+        s3.close()
+
+    cb = cpu_baseline(args.workload) if (rank == 0 and ws == 1 and not args.no_cpu) else None
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
+            "precision": ("FP32-mixed: FP32 derivative/RHS/flux/filter arithmetic; FP64 state, RK "
+                          "accumulation and Sherman-Morrison factor") if args.precision == "mixed"
+                         else "FP64 throughout",
+            "data": "synthetic",
+            "config": {"workload": desc, "npts": npts, "rk_stages": stages,
+                       "l2": "inputs larger than L2: the stage streams ~0.5-0.9 GB through HBM",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+            "clocks": clocks, "roofline": roofline, "cpu_baseline": cb,
+            "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": 5 * 8 * npts,
+                    "d2h_bytes_per_step": 5 * 8 * npts},
+            "gpu_launches": int(launches)}
+    line.update(other)
+    s.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tgv128", choices=["tgv128", "tgv64", "hit256", "shear"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the other form and the KE error")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

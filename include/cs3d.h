@@ -1,0 +1,206 @@
+/*
+ * cs3d.h -- C ABI of the GB300 implementation of the per-Runge-Kutta-stage
+ * path of 3DCompactSolver (compact derivatives, compact filter, Euler and
+ * viscous right-hand side, RK4 / TVD-RK3 stage update).
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (CS3D_OK on success).  Host pointers are caller-owned; device pointers
+ * ("_dev") must point to memory on the handle's GPU.  One handle owns one CUDA
+ * stream; calls on one handle must come from one host thread at a time, as
+ * with the reference's single-threaded driver loop.
+ *
+ * Citations are to files of the reference project (emathew1/3DCompactSolver).
+ */
+#ifndef CS3D_H
+#define CS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define CS3D_OK          0
+#define CS3D_ERR_ARG     1  /* null pointer, bad enum, bad index            */
+#define CS3D_ERR_SHAPE   2  /* grid too small for the requested closure     */
+#define CS3D_ERR_CUDA    3  /* a CUDA call failed (cs3d_last_error says which) */
+#define CS3D_ERR_NAN     4  /* a non-finite value reached the state         */
+#define CS3D_ERR_ALLOC   5  /* device or host allocation failed             */
+#define CS3D_ERR_STATE   6  /* call made in the wrong order                 */
+#define CS3D_ERR_NODEV   7  /* no CUDA device visible                       */
+
+/* ---- enumerations (values equal the reference's enums) ---------------- */
+/* BC::BCType, BC.hpp:10 */
+#define CS3D_PERIODIC_SOLVE   0
+#define CS3D_DIRICHLET_SOLVE  1
+/* BC::BCKind, BC.hpp:11 */
+#define CS3D_PERIODIC               0
+#define CS3D_SPONGE                 1
+#define CS3D_ADIABATIC_WALL         2
+#define CS3D_MOVING_ADIABATIC_WALL  3
+#define CS3D_INLET                  4
+/* Derivatives::Direct, Derivatives.hpp:48 */
+#define CS3D_DIRX 0
+#define CS3D_DIRY 1
+#define CS3D_DIRZ 2
+/* time integrators: RK4.hpp, TVDRK3.hpp */
+#define CS3D_RK4     0
+#define CS3D_TVDRK3  1
+/* arithmetic of the stage */
+#define CS3D_FP64        0  /* plain form: every operation in FP64        */
+#define CS3D_FP32_MIXED  1  /* RHS, flux, derivative and filter arithmetic in
+                               FP32; conserved state, RK accumulation and the
+                               cyclic Sherman-Morrison factor in FP64       */
+/* sponge construction */
+#define CS3D_SPONGE_REFERENCE 0 /* sigma built only on SPONGE faces with the
+                                   reference's band widths 0.25Lx, 0.125Ly,
+                                   0.25Lz (SpongeBC.hpp:56-62)             */
+#define CS3D_SPONGE_BANDS     1 /* sigma built on every face whose entry of
+                                   sponge_frac is > 0, band = frac * L      */
+
+/* Solver configuration.  Mirrors the constructor arguments of Domain
+ * (Domain.hpp:16), BC (BC.hpp:16), TimeStepping (TimeStepping.hpp:20) and
+ * CSolver_AWS (CSolver_AWS.hpp:119), plus the choice of integrator. */
+typedef struct cs3d_config {
+    int    Nx, Ny, Nz;          /* grid points per direction                */
+    double Lx, Ly, Lz;          /* x_i = i*L/(N-1), Domain.hpp:31-41        */
+    int    bc_type[3];          /* CS3D_PERIODIC_SOLVE / CS3D_DIRICHLET_SOLVE */
+    int    bc_kind[6];          /* faces X0,X1,Y0,Y1,Z0,Z1: CS3D_PERIODIC..  */
+    double alphaF;              /* compact filter coefficient               */
+    double mu_ref;              /* reference viscosity, IdealGas.hpp:40     */
+    double CFL;                 /* constant-CFL time step                   */
+    double dt_fixed;            /* > 0: frozen dt (adjoint); else CFL rule  */
+    int    filter_step;         /* filter when timeStep % filter_step == 0  */
+    int    rk;                  /* CS3D_RK4 / CS3D_TVDRK3                   */
+    int    precision;           /* CS3D_FP64 / CS3D_FP32_MIXED              */
+    int    sponge_mode;         /* CS3D_SPONGE_REFERENCE / CS3D_SPONGE_BANDS */
+    double sponge_frac[6];      /* band fraction per face (SPONGE_BANDS)    */
+    /* moving-wall velocities, CSolver_AWS.hpp:104-106, in the order
+     * X0V X0W X1V X1W Y0U Y0W Y1U Y1W Z0U Z0V Z1U Z1V */
+    double wall_vel[12];
+} cs3d_config;
+
+/* Fields addressable by cs3d_get_field / cs3d_set_field.  Conserved fields
+ * follow AbstractCSolver.hpp:19-26; primitives CSolver_AWS.hpp:40-48. */
+#define CS3D_F_RHO1   0
+#define CS3D_F_RHOU1  1
+#define CS3D_F_RHOV1  2
+#define CS3D_F_RHOW1  3
+#define CS3D_F_RHOE1  4
+#define CS3D_F_RHOK   5   /* rhok..rhoEk: stage input (qk)      5..9  */
+#define CS3D_F_RHO2   10  /* rho2..rhoE2: RK accumulator (q2)  10..14 */
+#define CS3D_F_RHOK2  15  /* rhok2..rhoEk2: last increment dq  15..19 */
+#define CS3D_F_U      20  /* U V W p T mu sos from q1 (the solver's
+                             primitives after the last stage)  20..26 */
+#define CS3D_F_SPONGE_AVG 27 /* sponge running averages        27..31 */
+#define CS3D_F_SIGMA  32
+#define CS3D_NUM_FIELDS 33
+
+typedef struct cs3d_handle cs3d_handle;
+
+/* Last error message of the calling thread (static storage). */
+const char *cs3d_last_error(void);
+
+/* Library version and the CUDA architecture it was built for. */
+int cs3d_version(int *major, int *minor, int *sm_arch);
+
+/* Create / destroy a solver on the current CUDA device.  Replaces
+ * `new CSolver_AWS(dom, bc, ts, alphaF, mu_ref, blocksize, useTiming)`
+ * (CSolver_AWS.hpp:119-185) plus initializeSolverData (CSolver_AWS.cpp:3-196).
+ * Device memory is allocated here and nowhere else. */
+int cs3d_create(const cs3d_config *cfg, cs3d_handle **out);
+int cs3d_destroy(cs3d_handle *h);
+
+/* Initial conditions from host arrays (XYZ layout, Nx*Ny*Nz doubles each).
+ * Replaces writing cs->rho0,p0,U0,V0,W0 and calling setInitialConditions
+ * (CSolver_AWS.cpp:199-504), including the wall overwrite, the sponge
+ * average initialisation and the primitive update. */
+int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, const double *p0,
+                                const double *U0, const double *V0, const double *W0);
+
+/* One time step: calcDtFromCFL (CSolver_AWS.cpp:507-551), every RK stage
+ * (RK4.hpp:120-170 / TVDRK3.hpp:98-139) and updateSponge
+ * (CSolver_AWS.cpp:1937-2031).  Diagnostics and file output of postStep are
+ * not part of the path. */
+int cs3d_step(cs3d_handle *h);
+/* Run n steps back to back with no host synchronisation in between. */
+int cs3d_run(cs3d_handle *h, int n);
+
+/* The pieces of cs3d_step, for drivers that call the reference's virtuals
+ * one by one (AbstractCSolver.hpp:36-43, AbstractRK.hpp:13-14). */
+int cs3d_pre_step(cs3d_handle *h);                            /* preStep      */
+int cs3d_sub_step(cs3d_handle *h, int rk_step, int rk_last);  /* preSubStep + solveEqnSet
+                                                                 + postSubStep
+                                                                 + updateConservedData
+                                                                 + updateData */
+int cs3d_post_step(cs3d_handle *h);                           /* updateSponge */
+
+/* Wait for all queued work; returns CS3D_ERR_NAN if the device status flag
+ * saw a non-finite value in the state since the last call. */
+int cs3d_sync(cs3d_handle *h);
+
+/* Copy a field (Nx*Ny*Nz doubles, XYZ layout) between host and device. */
+int cs3d_get_field(cs3d_handle *h, int field, double *host_out);
+int cs3d_set_field(cs3d_handle *h, int field, const double *host_in);
+/* Device pointer of a field (XYZ layout, FP64), valid until destroy. */
+int cs3d_field_ptr(cs3d_handle *h, int field, double **dev_ptr);
+
+/* Scalars: time step dt, simulated time, time-step counter
+ * (CSolver_AWS.hpp:28-31, TimeStepping.hpp:15). */
+int cs3d_get_scalars(cs3d_handle *h, double *dt, double *time, int *time_step);
+/* The CUDA stream the handle launches on (a cudaStream_t). */
+int cs3d_get_stream(cs3d_handle *h, void **stream);
+/* Number of kernels the handle has launched so far. */
+int cs3d_launch_count(cs3d_handle *h, long long *count);
+
+/* Options (value 0 = off, the default):
+ *  CS3D_OPT_STORE_INCREMENTS  keep the stage increments dt*RHS (rhok2..rhoEk2,
+ *                             CSolver_AWS.cpp:1246-1504) in device memory;
+ *  CS3D_OPT_STORE_DIAGNOSTICS keep Uz, Vz, Wz of the last stage so that
+ *                             cs3d_tgv_quantities can run. */
+#define CS3D_OPT_STORE_INCREMENTS  1
+#define CS3D_OPT_STORE_DIAGNOSTICS 2
+#define CS3D_OPT_KERNEL_TIMING     3  /* bracket every launch with CUDA events */
+int cs3d_set_option(cs3d_handle *h, int option, int value);
+
+/* Kernel classes of cs3d_kernel_times. */
+#define CS3D_K_SWEEP_X  0
+#define CS3D_K_SWEEP_Y  1
+#define CS3D_K_SWEEP_Z  2   /* z sweep + RHS + RK update */
+#define CS3D_K_FILTER   3
+#define CS3D_K_BOUNDARY 4
+#define CS3D_K_CFL      5
+#define CS3D_K_SPONGE   6
+#define CS3D_K_OTHER    7
+#define CS3D_NUM_KERNEL_CLASSES 8
+/* Accumulated device time (ms, from CUDA events on the handle's stream) and
+ * launch count per kernel class while CS3D_OPT_KERNEL_TIMING was on; waits
+ * for the recorded work.  reset != 0 clears the totals afterwards.  No
+ * counterpart in the reference (its useTiming flag prints host wall time per
+ * phase, CSolver_AWS.cpp:1237-1240). */
+int cs3d_kernel_times(cs3d_handle *h, double *ms, long long *count, int n, int reset);
+
+/* ---- single operators on device arrays --------------------------------
+ * Replace Derivatives::calc1stDerivField / calc2ndDerivField
+ * (Derivatives.hpp:167-168, Derivatives.cpp:3-96) and Filter::filterField
+ * (Filter.hpp:115, Filter.cpp:129-171).  As in the reference, `in` holds the
+ * field in the direction's contiguous layout (DIRX: XYZ, DIRY: YZX,
+ * DIRZ: ZXY, Macros.hpp:8-10): lines of length N_dir, one after another.
+ * FP64 in and out; `in` and `out` must not overlap. */
+int cs3d_deriv1(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
+int cs3d_deriv2(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
+int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
+
+/* Kinetic energy and dissipation diagnostics of the Taylor-Green case,
+ * the columns of calcTaylorGreenQuantities (CSolver_AWS.cpp:2175-2257):
+ * out[0..6] = time, KEsum, dissSum, enstrophySum, enstrophy*2mu, meanMu,
+ * dilprime.  Derivatives are those of the last stage, as in the reference;
+ * requires CS3D_OPT_STORE_DIAGNOSTICS to have been on during that stage. */
+int cs3d_tgv_quantities(cs3d_handle *h, double out[7]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CS3D_H */

@@ -1,0 +1,57 @@
+"""Shared fixtures.  GPU tests carry @pytest.mark.gpu; everything else runs
+on the CPU.  The oracle (oracle/) is the checker: tests may call it, the
+product never does."""
+import importlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs through the C ABI")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    import oracle as o
+    o.build()
+    return o
+
+
+@pytest.fixture(scope="session")
+def pkg():
+    return importlib.import_module("3dcompactsolver_gb300")
+
+
+@pytest.fixture(scope="session")
+def cases():
+    return importlib.import_module("3dcompactsolver_gb300.cases")
+
+
+@pytest.fixture(scope="session")
+def gpu_pkg(pkg):
+    """The package with its CUDA library built; fails (never skips) when the
+    library cannot be built or loaded on a GPU machine."""
+    b = importlib.import_module("3dcompactsolver_gb300.build")
+    b.build()
+    pkg.lib()
+    return pkg
+
+
+def rel_err(a, b):
+    """Relative max-norm error of a against b, per field (last 3 axes)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    den = np.abs(b).max()
+    return float(np.abs(a - b).max() / (den if den > 0 else 1.0))
+
+
+def load_golden(name):
+    return np.load(os.path.join(GOLDEN, name))

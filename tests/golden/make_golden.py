@@ -1,0 +1,81 @@
+"""Regenerate the golden fixtures of tests/golden from the reference.
+
+Needs the reference checkout (default /root/reference, or $CS3D_REFERENCE)
+and the reference harness built by `make -C oracle ref`.  Writes:
+
+  taylorgreen_run64_head.txt   rows 1-5 of taylorgreen_vortex/taylorgreen_run64/taylorgreen.out
+  taylorgreen_run128_head.txt  rows 1-3 of taylorgreen_vortex/taylorgreen_run128/taylorgreen.out
+  ref_<case>.npz               q1 after 3 steps of the reference's own CSolver_AWS + RK4/TVDRK3
+                               (oracle/_ref, strict build), with dt, time and timeStep
+  ref_lineops.npz              the reference's calc1stDerivField / calc2ndDerivField /
+                               filterField on seeded random fields
+
+Run:  python tests/golden/make_golden.py
+"""
+import importlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle  # noqa: E402
+
+REF = os.environ.get("CS3D_REFERENCE", "/root/reference")
+cases = importlib.import_module("3dcompactsolver_gb300.cases")
+_abi = importlib.import_module("3dcompactsolver_gb300._abi")
+
+# Small cases: every boundary kind, both integrators, sponge faces and bands.
+CASES = {
+    "tgv12": lambda: cases.tgv(12),
+    "wall": lambda: cases.wall_box((12, 10, 9)),
+    "wall_moving_sponge": lambda: cases.wall_box((12, 10, 9), moving=True, sponge=True),
+    "wall_tvdrk3": lambda: cases.wall_box((12, 10, 9), rk=_abi.TVDRK3),
+    "shear": lambda: cases.shear_layer(16, 12, 10, precision=_abi.FP64),
+}
+NSTEPS = 3
+
+# single operators: (kind, dir, bc_type, (Nx, Ny, Nz))
+LINEOPS = [(k, d, bc, n) for k in (1, 2, 3) for d in (0, 1, 2) for bc in (0, 1)
+           for n in [(12, 10, 9)]] + [(k, 0, bc, (37, 3, 2)) for k in (1, 2, 3) for bc in (0, 1)]
+
+
+def main():
+    for N, rows in ((64, 5), (128, 3)):
+        src = os.path.join(REF, f"taylorgreen_vortex/taylorgreen_run{N}/taylorgreen.out")
+        with open(src) as f:
+            lines = [next(f) for _ in range(rows)]
+        with open(os.path.join(HERE, f"taylorgreen_run{N}_head.txt"), "w") as f:
+            f.writelines(lines)
+    oracle.build(ref=True)
+    for name, mk in CASES.items():
+        cfg, ic = mk()
+        r = oracle.RefSolver(cfg)
+        r.set_initial_conditions(*ic)
+        for _ in range(NSTEPS):
+            r.step()
+        dt, t, ts = r.scalars()
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), q1=r.conserved(), dt=dt, time=t,
+                            timeStep=ts, nsteps=NSTEPS)
+    rng = np.random.default_rng(2024)
+    out = {}
+    for idx, (kind, d, bc, n) in enumerate(LINEOPS):
+        Nd = n[d]
+        nl = n[0] * n[1] * n[2] // Nd
+        x = rng.standard_normal((nl, Nd)) + np.sin(np.linspace(0, 3, Nd))[None, :]
+        L = (3.0, 2.5, 2.0)
+        y = oracle.line_op_ref(kind, d, bc, n, L, 0.47, x)
+        out[f"in{idx}"] = x
+        out[f"out{idx}"] = y
+        out[f"meta{idx}"] = np.array([kind, d, bc, n[0], n[1], n[2]])
+    out["L"] = np.array([3.0, 2.5, 2.0])
+    out["alphaF"] = np.array(0.47)
+    np.savez_compressed(os.path.join(HERE, "ref_lineops.npz"), **out)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,55 @@
+"""The FP32-mixed form: kinetic-energy error against the FP64 form, and
+stability on every workload shape."""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ke(q):
+    return float(0.5 * np.sum((q[1] ** 2 + q[2] ** 2 + q[3] ** 2) / q[0]))
+
+
+def test_tgv_mixed_ke_error(gpu_pkg, cases):
+    """TGV 32^3, 40 RK4 steps: |KE_mixed - KE_fp64| / KE_fp64 < 1e-5."""
+    abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    out = {}
+    for prec in (abi.FP64, abi.FP32_MIXED):
+        cfg, ic = cases.tgv(32, precision=prec)
+        s = gpu_pkg.Solver(cfg)
+        s.set_initial_conditions(*ic)
+        s.run(40)
+        s.sync()
+        out[prec] = s.conserved()
+        s.close()
+    ke64, ke32 = _ke(out[abi.FP64]), _ke(out[abi.FP32_MIXED])
+    assert abs(ke32 - ke64) / ke64 < 1e-5, (ke32, ke64)
+    for f in range(5):
+        d = np.abs(out[abi.FP32_MIXED][f] - out[abi.FP64][f]).max() / np.abs(out[abi.FP64][f]).max()
+        assert d < 1e-4, (f, d)
+
+
+@pytest.mark.parametrize("name", ["wall_moving_sponge", "shear", "hit"])
+def test_mixed_tracks_fp64(gpu_pkg, cases, name):
+    abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    mk = {
+        "wall_moving_sponge": lambda p: cases.wall_box((20, 16, 12), moving=True, sponge=True, precision=p),
+        "shear": lambda p: cases.shear_layer(32, 24, 16, precision=p),
+        "hit": lambda p: cases.hit(32, precision=p),
+    }[name]
+    out = {}
+    for prec in (abi.FP64, abi.FP32_MIXED):
+        cfg, ic = mk(prec)
+        s = gpu_pkg.Solver(cfg)
+        s.set_initial_conditions(*ic)
+        s.run(15)
+        s.sync()
+        out[prec] = s.conserved()
+        s.close()
+    for f in range(5):
+        a, b = out[abi.FP32_MIXED][f], out[abi.FP64][f]
+        assert np.isfinite(a).all()
+        d = np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+        assert d < 1e-4, (name, f, d)
