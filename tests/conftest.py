@@ -45,12 +45,22 @@ def gpu_pkg(pkg):
     return pkg
 
 
-def rel_err(a, b):
-    """Relative max-norm error of a against b, per field (last 3 axes)."""
+def rel_err(a, b, scale=None):
+    """Relative max-norm error max|a-b| / max|b| of one field; `scale`
+    replaces max|b| where a field's own maximum is not its natural size."""
     a = np.asarray(a)
     b = np.asarray(b)
-    den = np.abs(b).max()
+    den = np.abs(b).max() if scale is None else scale
     return float(np.abs(a - b).max() / (den if den > 0 else 1.0))
+
+
+def state_errors(q, qr):
+    """Per conserved field relative max-norm errors of q against qr (both
+    (5, Nz, Ny, Nx)).  Density and energy are measured against their own
+    maxima; the three momenta against the largest momentum component, since a
+    component can start at zero (w of the Taylor-Green vortex)."""
+    mom = max(float(np.abs(qr[f]).max()) for f in (1, 2, 3))
+    return [rel_err(q[f], qr[f], mom if f in (1, 2, 3) else None) for f in range(5)]
 
 
 def load_golden(name):
