@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <cstdlib>
 
 #include "../../include/cs3d.h"
 #include "cs3d_dev.cuh"
@@ -195,22 +196,33 @@ struct DevOp {
 
 template <typename T>
 int upload_op(const HostOp &h, DevOp<T> &d, cudaStream_t s) {
-    int N = h.N;
-    std::vector<T> buf(4 * (size_t)N);
+    const int N = h.N;
+    // seven arrays of S elements each (S a multiple of 4, with at least 8
+    // elements of zero padding so chunked loads never leave an array)
+    const size_t S = ((size_t)N + 8 + 3) & ~(size_t)3;
+    std::vector<T> buf(7 * S, T(0));
     for (int i = 0; i < N; i++) {
         buf[i] = (T)h.m[i];
-        buf[N + i] = (T)h.iw[i];
-        buf[2 * N + i] = (T)h.c[i];
-        buf[3 * N + i] = (T)h.z[i];
+        buf[S + i] = (T)h.iw[i];
+        buf[2 * S + i] = (T)h.c[i];
+        buf[3 * S + i] = (T)h.z[i];
     }
-    CS3D_CUDA(cudaMalloc(&d.mem, sizeof(T) * 4 * (size_t)N));
-    CS3D_CUDA(cudaMemcpyAsync(d.mem, buf.data(), sizeof(T) * 4 * (size_t)N, cudaMemcpyHostToDevice, s));
+    for (int k = 0; k + h.H < N; k++) buf[4 * S + k] = (T)h.m[k + h.H];
+    for (int k = 0; k <= N - 2; k++) {
+        buf[5 * S + k] = (T)h.c[N - 2 - k];
+        buf[6 * S + k] = (T)h.iw[N - 2 - k];
+    }
+    CS3D_CUDA(cudaMalloc(&d.mem, sizeof(T) * buf.size()));
+    CS3D_CUDA(cudaMemcpyAsync(d.mem, buf.data(), sizeof(T) * buf.size(), cudaMemcpyHostToDevice, s));
     CS3D_CUDA(cudaStreamSynchronize(s));
     LineOp<T> &o = d.op;
     o.m = d.mem;
-    o.iw = d.mem + N;
-    o.c = d.mem + 2 * N;
-    o.z = d.mem + 3 * N;
+    o.iw = d.mem + S;
+    o.c = d.mem + 2 * S;
+    o.z = d.mem + 3 * S;
+    o.mf = d.mem + 4 * S;
+    o.cbk = d.mem + 5 * S;
+    o.ibk = d.mem + 6 * S;
     for (int k = 0; k < kTaps; k++) o.taps[k] = (T)h.taps[k];
     for (int b = 0; b < 2 * kMaxH; b++) {
         for (int k = 0; k < kTaps; k++) o.btaps[b][k] = (T)h.btaps[b][k];
@@ -253,8 +265,10 @@ struct cs3d_handle {
     int nstages = 4;
     int mixed = 0;
     size_t tb = 8;  // bytes of the work type
-    // conserved state
+    // conserved state, and its FP32 shadows in the mixed form
     Q5 q1{}, qk{}, q2{};
+    float *q1s[5] = {}, *qks[5] = {}, *q2s[5] = {};
+    int mixed_rk4 = 0;  // mixed form with RK4: the stage input qk lives in qks only
     double *dq[5] = {};
     // work-precision fields (double or float, by tb)
     void *prim[5] = {}, *mu = nullptr, *amu = nullptr, *dx4[4] = {}, *dy4[4] = {}, *R[5] = {}, *diag[3] = {};
@@ -400,10 +414,17 @@ static int check_config(const cs3d_config *c) {
     return CS3D_OK;
 }
 
-// Tile width: the widest power of two (<= 32 lines) whose shared memory fits
-// three blocks per SM.
+// Tile width: the widest power of two (<= 32 lines) whose shared memory
+// stays within the per-block budget: 40 KB in the mixed form (five blocks per
+// SM, so one block's loads overlap another's solves), 72 KB in the plain form
+// (FP64-throughput bound; three blocks per SM keep the FP64 pipe busy).
+// CS3D_SMEM_BUDGET_KB overrides the budget.
 static int pick_L(size_t tb, int nbuf, int N, int pitch_plus) {
-    const size_t budget = 72 * 1024;
+    size_t budget = (tb == 4 ? 40 : 72) * 1024;
+    if (const char *e = getenv("CS3D_SMEM_BUDGET_KB")) {
+        long v = strtol(e, nullptr, 10);
+        if (v >= 8 && v <= 220) budget = (size_t)v * 1024;
+    }
     int L = 32;
     while (L > 1 && sweep_smem_bytes((int)tb, nbuf, L, L + pitch_plus, N) > budget) L /= 2;
     return L;
@@ -492,6 +513,14 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         ALLOC(h->dx4[f], n * h->tb);
         ALLOC(h->dy4[f], n * h->tb);
     }
+    if (h->mixed) {
+        h->mixed_rk4 = cfg->rk == CS3D_RK4;
+        for (int f = 0; f < 5; f++) {
+            ALLOC(h->q1s[f], n * 4);
+            ALLOC(h->qks[f], n * 4);
+            ALLOC(h->q2s[f], n * 4);
+        }
+    }
     ALLOC(h->mu, n * h->tb);
     ALLOC(h->amu, n * h->tb);
     ALLOC(h->scal, 8 * sizeof(double));
@@ -521,6 +550,8 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
     for (int d = 0; d < 3; d++) {
         h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
         h->Lf[d] = pick_L(h->tb, 5, Nd[d], d == 0 ? 1 : 0);
+        if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
+            return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
     h->threads = 128;
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
@@ -552,12 +583,26 @@ extern "C" int cs3d_destroy(cs3d_handle *h) {
 // ---------------------------------------------------------------------
 // launches
 // ---------------------------------------------------------------------
+static int launch_shadow_of(cs3d_handle *h, const Q5 &q, float *const out[5]) {
+    ShadowArgs a{};
+    a.g = h->g;
+    a.q = q;
+    for (int f = 0; f < 5; f++) a.out[f] = out[f];
+    a.nf = 5;
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_shadow(a, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
 static int launch_cfl_reduce(cs3d_handle *h) {
     CS3D_CUDA(cudaMemsetAsync(h->scal + 2, 0, sizeof(double), h->stream));
     CflArgs a{};
     a.g = h->g;
     a.gas = h->gas;
     a.q = h->q1;
+    if (h->mixed)
+        for (int f = 0; f < 5; f++) a.qs[f] = h->q1s[f];
     a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
     a.max_out = h->scal + 2;
     a.nan_flag = h->flag;
@@ -616,6 +661,10 @@ extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, c
         }
     }
     CS3D_CUDA(cudaFree(tmp));
+    if (h->mixed) {
+        int r = launch_shadow_of(h, h->q1, h->q1s);
+        if (r) return r;
+    }
     h->timeStep = 0;
     h->filterTimeStep = 0;
     h->backup_valid = 0;
@@ -647,14 +696,23 @@ extern "C" int cs3d_pre_step(cs3d_handle *h) {
 
 template <typename T>
 static int run_stage(cs3d_handle *h, int st, int last) {
-    const Q5 qs = st == 1 ? h->q1 : h->qk;
+    // stage input q*: q1 on stage 1, qk afterwards (RK4.hpp:133-137); in the
+    // mixed RK4 form qk exists only as its FP32 shadow
+    const bool qk_shadow_only = h->mixed_rk4 && st > 1;
+    const Q5 qin = st == 1 ? h->q1 : (qk_shadow_only ? Q5{} : h->qk);
+    float *const *qin32 = st == 1 ? h->q1s : h->qks;
     const int use_backup = st == 1 && h->backup_valid;
+    const bool filtered = h->timeStep % h->cfg.filter_step == 0;
     // walls before the derivatives
     if (h->wall_faces) {
         BCArgs b{};
         b.g = h->g;
         b.gas = h->gas;
-        b.q = qs;
+        b.q = qin;
+        for (int f = 0; f < 5; f++) {
+            b.qs[f] = h->mixed ? qin32[f] : nullptr;
+            b.qs_out[f] = h->mixed ? qin32[f] : nullptr;
+        }
         b.backup = h->backup;
         b.use_backup = use_backup;
         b.wall_faces = h->wall_faces;
@@ -675,16 +733,17 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.g = h->g;
     a.threads = h->threads;
     a.gas = h->gas;
-    a.q = qs;
+    a.q = qin;
+    for (int f = 0; f < 5; f++) a.qs[f] = h->mixed ? (const T *)qin32[f] : (const T *)qin.f[f];
     a.backup = h->backup;
     a.use_backup = use_backup;
     a.wall_faces = h->wall_faces;
-    a.sponge_faces = h->sponge_kind_faces;
     a.sponge_kind_faces = h->sponge_kind_faces;
     for (int f = 0; f < 5; f++) {
         a.prim[f] = (T *)h->prim[f];
         a.R[f] = (T *)h->R[f];
         a.dq_out[f] = h->store_dq ? h->dq[f] : nullptr;
+        a.q1s[f] = h->q1s[f];
     }
     a.mu = (T *)h->mu;
     a.amu = (T *)h->amu;
@@ -693,13 +752,21 @@ static int run_stage(cs3d_handle *h, int st, int last) {
         a.dy[f] = (T *)h->dy4[f];
     }
     for (int f = 0; f < 3; f++) a.diag[f] = h->store_diag ? (T *)h->diag[f] : nullptr;
-    if (!h->store_diag) a.diag[0] = nullptr;
     a.dt = h->scal;
     a.rk = h->cfg.rk == CS3D_TVDRK3 ? 1 : 0;
     a.rk_step = st;
     a.q1 = h->q1;
     a.q2 = h->q2;
     a.qk = h->qk;
+    a.mixed_rk4 = h->mixed_rk4;
+    // FP32 shadow written by the z sweep: the next stage's input, or -- after
+    // the last stage of a step that is not filtered -- q2, which becomes q1
+    a.shadow_target = SHADOW_NONE;
+    if (h->mixed) {
+        if (!last) a.shadow_target = SHADOW_QK;
+        else if (!filtered) a.shadow_target = SHADOW_Q2;
+        for (int f = 0; f < 5; f++) a.shadow_out[f] = last ? h->q2s[f] : h->qks[f];
+    }
     a.sponge = h->sponge;
     a.sigma = h->sigma;
     a.savg = h->savg;
@@ -718,7 +785,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
         tend(h);
     }
     if (last) {
-        if (h->timeStep % h->cfg.filter_step == 0) {
+        if (filtered) {
             // filterConservedData round robin (CSolver_AWS.cpp:1690-1863)
             h->filterTimeStep++;
             int order[3];
@@ -744,13 +811,16 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                     fa.dst64.f[f] = pass == 2 ? h->q1.f[f] : nullptr;
                     fa.dst32[f] = pass == 2 ? nullptr : (T *)dst[f];
                     fa.delta_from.f[f] = (pass == 2 && h->mixed) ? h->q2.f[f] : nullptr;
+                    fa.shadow_out[f] = (pass == 2 && h->mixed) ? h->q1s[f] : nullptr;
                 }
                 tstart(h, CS3D_K_FILTER);
                 CS3D_CUDA(launch_filter<T>(d, fa, h->stream));
                 tend(h);
             }
         } else {
+            // not a filter step: q1 takes q2's values (:1866-1880) by exchange
             std::swap(h->q1, h->q2);
+            for (int f = 0; f < 5; f++) std::swap(h->q1s[f], h->q2s[f]);
         }
         int rc = launch_cfl_reduce(h);
         if (rc) return rc;
@@ -781,6 +851,7 @@ extern "C" int cs3d_post_step(cs3d_handle *h) {
     a.q1 = h->q1;
     a.savg = h->savg;
     a.backup = h->backup;
+    for (int f = 0; f < 5; f++) a.q1s[f] = h->mixed ? h->q1s[f] : nullptr;
     a.sponge_kind_faces = h->sponge_kind_faces;
     tstart(h, CS3D_K_SPONGE);
     CS3D_CUDA(launch_sponge_update(a, h->stream));
@@ -833,7 +904,19 @@ extern "C" int cs3d_sync(cs3d_handle *h) {
 static int field_ptr(cs3d_handle *h, int field, double **p) {
     *p = nullptr;
     if (field >= CS3D_F_RHO1 && field < CS3D_F_RHO1 + 5) *p = h->q1.f[field - CS3D_F_RHO1];
-    else if (field >= CS3D_F_RHOK && field < CS3D_F_RHOK + 5) *p = h->qk.f[field - CS3D_F_RHOK];
+    else if (field >= CS3D_F_RHOK && field < CS3D_F_RHOK + 5) {
+        *p = h->qk.f[field - CS3D_F_RHOK];
+        if (h->mixed_rk4) {
+            // the mixed RK4 form keeps the stage input qk as an FP32 shadow only
+            ShadowArgs a{};
+            a.g = h->g;
+            a.q.f[0] = *p;
+            a.in[0] = h->qks[field - CS3D_F_RHOK];
+            a.nf = 1;
+            CS3D_CUDA(launch_shadow(a, h->stream));
+            h->launches++;
+        }
+    }
     else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) *p = h->q2.f[field - CS3D_F_RHO2];
     else if (field >= CS3D_F_RHOK2 && field < CS3D_F_RHOK2 + 5) {
         if (!h->store_dq) return fail(CS3D_ERR_STATE, "increments are kept only with CS3D_OPT_STORE_INCREMENTS");
@@ -880,6 +963,18 @@ extern "C" int cs3d_set_field(cs3d_handle *h, int field, const double *host_in) 
     int rc = field_ptr(h, field, &p);
     if (rc) return rc;
     CS3D_CUDA(cudaMemcpyAsync(p, host_in, (size_t)h->g.npts * 8, cudaMemcpyHostToDevice, h->stream));
+    if (h->mixed && field < CS3D_F_RHOK2) {
+        // keep the FP32 shadow of the written state in step
+        const int grp = field / 5, f = field % 5;
+        float *out = (grp == 0 ? h->q1s : grp == 1 ? h->qks : h->q2s)[f];
+        ShadowArgs a{};
+        a.g = h->g;
+        a.q.f[0] = p;
+        a.out[0] = out;
+        a.nf = 1;
+        CS3D_CUDA(launch_shadow(a, h->stream));
+        h->launches++;
+    }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }

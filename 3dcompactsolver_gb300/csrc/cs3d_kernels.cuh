@@ -13,6 +13,9 @@ struct GasParams {
     double mu_ref;
 };
 
+// What the z sweep writes as the FP32 shadow of the next stage's input.
+enum ShadowTarget { SHADOW_NONE = 0, SHADOW_QK = 1, SHADOW_Q2 = 2 };
+
 template <typename T>
 struct SweepArgs {
     Geom g;
@@ -21,12 +24,13 @@ struct SweepArgs {
     int threads;    // threads per block
     LineOp<T> d1, d2;
     GasParams gas;
-    Q5 q;           // stage input q* (FP64)
+    const T *qs[5]; // stage input q* in the work precision (FP64 q* itself, or
+                    // its FP32 shadow in the mixed form)
+    Q5 q;           // stage input q* (FP64; the mixed RK4 form keeps qk in FP32 only)
     Q5 backup;      // q1 before the last sponge overwrite (SPONGE faces)
     int use_backup; // stage 1 after a sponge overwrite
     int wall_faces;         // bit per face: wall (adiabatic or moving)
-    int sponge_faces;       // bit per face: SPONGE kind (for the backup rule)
-    int sponge_kind_faces;  // bit per face: SPONGE kind (increments zeroed)
+    int sponge_kind_faces;  // bit per face: SPONGE kind
     T *prim[5];     // U V W p T of q*
     T *mu, *amu;    // mu(T), dmu/dT
     T *dx[4];       // Ux Vx Wx Tx
@@ -37,6 +41,10 @@ struct SweepArgs {
     const double *dt;
     int rk, rk_step;
     Q5 q1, q2, qk;
+    const float *q1s[5];    // FP32 shadow of q1 (mixed RK4, stages 2-3)
+    float *shadow_out[5];   // FP32 shadow of the next stage input (mixed)
+    int shadow_target;      // ShadowTarget
+    int mixed_rk4;          // mixed form with RK4: qk kept only as FP32 shadow
     int sponge;
     const double *sigma;
     Q5 savg;
@@ -53,6 +61,7 @@ struct FilterArgs {
     Q5 dst64;          // FP64 destination (or null pointers)
     T *dst32[5];       // work-precision destination
     Q5 delta_from;     // mixed last pass: q1 = q2 + (filtered - unfiltered)
+    float *shadow_out[5];  // mixed last pass: FP32 shadow of q1
     double ref[5];     // per-field reference value subtracted on entry
 };
 
@@ -69,7 +78,9 @@ struct BCArgs {
     int face;
     double uw[3];
     GasParams gas;
-    Q5 q;
+    Q5 q;                 // stage input (FP64)
+    const float *qs[5];   // ... or its FP32 shadow, when q holds null pointers
+    float *qs_out[5];     // FP32 shadow to update (mixed)
     Q5 backup;
     int use_backup;
     int wall_faces, sponge_faces;
@@ -79,6 +90,7 @@ struct CflArgs {
     Geom g;
     GasParams gas;
     Q5 q;
+    const float *qs[5];   // mixed: the FP32 shadow of q1 instead of q
     double dx, dy, dz;
     double *max_out;
     int *nan_flag;
@@ -96,6 +108,7 @@ struct SpongeArgs {
     const double *dt;
     double avgT, epsP, spongeP, gm1;
     Q5 q1, savg, backup;
+    float *q1s[5];  // FP32 shadow of q1 to keep in step (mixed)
     int sponge_kind_faces;
 };
 
@@ -116,6 +129,14 @@ struct PrimArgs {
     double *out[7];
 };
 
+struct ShadowArgs {
+    Geom g;
+    Q5 q;
+    float *out[5];
+    const float *in[5];
+    int nf;
+};
+
 template <typename T>
 struct TgvArgs {
     Geom g;
@@ -126,12 +147,12 @@ struct TgvArgs {
 };
 
 template <typename T>
-cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s);
-template <typename T>
 cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s);
 cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s);
 cudaError_t launch_wall_pre(const BCArgs &a, cudaStream_t s);
 cudaError_t launch_cfl(const CflArgs &a, cudaStream_t s);
 cudaError_t launch_nan_scan(const CflArgs &a, cudaStream_t s);
@@ -141,9 +162,11 @@ cudaError_t launch_ic(const IcArgs &a, cudaStream_t s);
 cudaError_t launch_ic_wall(const IcArgs &a, cudaStream_t s);
 cudaError_t launch_ic_wall_eos(const IcArgs &a, cudaStream_t s);
 cudaError_t launch_primitives(const PrimArgs &a, cudaStream_t s);
+cudaError_t launch_shadow(const ShadowArgs &a, cudaStream_t s);
 
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N);
 int sweep_nbuf(int dir);
 int sweep_ntask(int dir);
+int filter_ntask();
 
 }  // namespace cs3d

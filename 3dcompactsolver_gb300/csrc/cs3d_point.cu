@@ -1,0 +1,386 @@
+// cs3d_point.cu -- pointwise and face kernels of the stage path (sm_103a):
+// wall boundary conditions, CFL reduction, sponge update, initial conditions,
+// diagnostics and the FP32 shadow of the state used by the mixed form.
+#include <cstdio>
+#include <cmath>
+#include "cs3d_dev.cuh"
+#include "cs3d_kernels.cuh"
+
+namespace cs3d {
+
+// ---------------------------------------------------------------------
+// wall boundary conditions before the derivatives (CSolver_AWS.cpp:553-826)
+// ---------------------------------------------------------------------
+// One launch per face, in the reference's order.  Temperatures of interior
+// points come from the current state; on stage 1, points of SPONGE faces that
+// are not on a wall use the state saved before the previous step's sponge
+// overwrite.  The state is FP64 (q), or only its FP32 shadow (qs) for the
+// stage input qk of the mixed RK4 form; a shadow in qs_out is kept in step.
+__device__ __forceinline__ double temp_at(const BCArgs &a, long long gi, int fc) {
+    double q[5];
+    const bool bk = a.use_backup && (fc & a.sponge_faces) && !(fc & a.wall_faces);
+#pragma unroll
+    for (int f = 0; f < 5; ++f)
+        q[f] = bk ? a.backup.f[f][gi] : (a.q.f[0] ? a.q.f[f][gi] : widen(a.qs[f][gi]));
+    const double r = q[0];
+    const double U = q[1] / r, V = q[2] / r, W = q[3] / r;
+    const double p = a.gas.gm1 * (q[4] - 0.5 * r * (U * U + V * V + W * W));
+    return p / (r * a.gas.R);
+}
+
+__global__ void k_wall_pre(BCArgs a) {
+    const Geom g = a.g;
+    const int dir = a.face / 2, hi = a.face % 2;
+    const int n1 = dir == 0 ? g.Ny : g.Nx, n2 = dir == 2 ? g.Ny : g.Nz;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n1 * n2) return;
+    const int a1 = (int)(idx % n1), a2 = (int)(idx / n1);
+    const int Nd = dir == 0 ? g.Nx : dir == 1 ? g.Ny : g.Nz;
+    const int fix = hi ? Nd - 1 : 0, sg = hi ? -1 : 1;
+    int i, j, k;
+    if (dir == 0) { i = fix; j = a1; k = a2; }
+    else if (dir == 1) { i = a1; j = fix; k = a2; }
+    else { i = a1; j = a2; k = fix; }
+    const long long nxy = (long long)g.Nx * g.Ny;
+    const long long gi = (long long)k * nxy + (long long)j * g.Nx + i;
+    const long long step = dir == 0 ? 1 : dir == 1 ? g.Nx : nxy;
+    double Tn[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        const long long nb = gi + sg * (m + 1) * step;
+        int ii = i, jj = j, kk = k;
+        if (dir == 0) ii += sg * (m + 1); else if (dir == 1) jj += sg * (m + 1); else kk += sg * (m + 1);
+        Tn[m] = temp_at(a, nb, faces_of(g, ii, jj, kk));
+    }
+    // Utils.hpp:52-54
+    const double Tw = (Tn[0] * 360.0 - Tn[1] * 450.0 + Tn[2] * 400.0 - Tn[3] * 225.0 + Tn[4] * 72.0 - Tn[5] * 10.0) / 147.0;
+    const double r = a.q.f[0] ? a.q.f[0][gi] : widen(a.qs[0][gi]);
+    double nq[5];
+    nq[0] = r;
+    nq[1] = dir == 0 ? 0.0 : r * a.uw[0];
+    nq[2] = dir == 1 ? 0.0 : r * a.uw[1];
+    nq[3] = dir == 2 ? 0.0 : r * a.uw[2];
+    const double p = r * a.gas.R * Tw;
+    nq[4] = p / a.gas.gm1 + 0.5 * r * (a.uw[0] * a.uw[0] + a.uw[1] * a.uw[1] + a.uw[2] * a.uw[2]);
+    if (a.q.f[0])
+        for (int f = 1; f < 5; ++f) a.q.f[f][gi] = nq[f];
+    if (a.qs_out[0])
+        for (int f = 1; f < 5; ++f) a.qs_out[f][gi] = narrow(nq[f]);
+}
+
+// ---------------------------------------------------------------------
+// CFL reduction (CSolver_AWS.cpp:507-525): max over points of
+// (|u|+c)/dx + (|v|+c)/dy + (|w|+c)/dz, kept as the bit pattern of a
+// positive double so atomicMax on 64-bit integers orders it.  FP64 from the
+// state, or FP32 from its shadow in the mixed form.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void block_max_commit(double mx, double *out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = mx;
+    __syncthreads();
+    if (wid == 0) {
+        mx = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) atomicMax(reinterpret_cast<unsigned long long *>(out), (unsigned long long)__double_as_longlong(mx));
+    }
+}
+
+__global__ void k_cfl(CflArgs a) {
+    double mx = 0.0;
+    int bad = 0;
+    if (a.qs[0]) {
+        float fm = 0.f;
+        const float gam = (float)a.gas.gamma, gm1 = (float)a.gas.gm1;
+        const float idx = (float)(1.0 / a.dx), idy = (float)(1.0 / a.dy), idz = (float)(1.0 / a.dz);
+        for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+             gi += (long long)gridDim.x * blockDim.x) {
+            const float r = a.qs[0][gi];
+            const float U = a.qs[1][gi] / r, V = a.qs[2][gi] / r, W = a.qs[3][gi] / r;
+            const float p = gm1 * (a.qs[4][gi] - 0.5f * r * (U * U + V * V + W * W));
+            const float c = sqrtf(gam * p / r);
+            const float v = (fabsf(U) + c) * idx + (fabsf(V) + c) * idy + (fabsf(W) + c) * idz;
+            bad |= !(v == v) || isinf(v);
+            fm = fmaxf(fm, v);
+        }
+        mx = widen(fm);
+    } else {
+        for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+             gi += (long long)gridDim.x * blockDim.x) {
+            const double r = a.q.f[0][gi];
+            const double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+            const double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
+            const double c = sqrt(a.gas.gamma * p / r);
+            const double v = (fabs(U) + c) / a.dx + (fabs(V) + c) / a.dy + (fabs(W) + c) / a.dz;
+            bad |= !(v == v) || isinf(v);
+            mx = fmax(mx, v);
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *a.nan_flag = 1;
+    block_max_commit(mx, a.max_out);
+}
+
+// dt = CFL / max and the step/time counters (CSolver_AWS.cpp:530-543).
+__global__ void k_finalize_dt(DtArgs a) {
+    double mx = *a.max_in;
+    double dt = a.dt_fixed > 0.0 ? a.dt_fixed : a.CFL / mx;
+    *a.dt = dt;
+    if (a.first) *a.time = 0.0;
+    else *a.time = *a.time + dt;
+}
+
+// ---------------------------------------------------------------------
+// updateSponge (CSolver_AWS.cpp:1937-2031)
+// ---------------------------------------------------------------------
+__global__ void k_sponge_update(SpongeArgs a) {
+    const double eps = 1.0 / (a.avgT / *a.dt + 1.0);
+    const long long nxy = (long long)a.g.Nx * a.g.Ny;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double av[5];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            double s = a.savg.f[f][gi];
+            s += eps * (a.q1.f[f][gi] - s);
+            av[f] = s;
+        }
+        av[4] = a.epsP * av[4] +
+                (1.0 - a.epsP) * (a.spongeP / a.gm1 + 0.5 * (av[1] * av[1] + av[2] * av[2] + av[3] * av[3]) / av[0]);
+#pragma unroll
+        for (int f = 0; f < 5; ++f) a.savg.f[f][gi] = av[f];
+        if (a.sponge_kind_faces) {
+            const int k = (int)(gi / nxy);
+            const long long rem = gi - k * nxy;
+            const int j = (int)(rem / a.g.Nx), i = (int)(rem - (long long)j * a.g.Nx);
+            if (faces_of(a.g, i, j, k) & a.sponge_kind_faces) {
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    a.backup.f[f][gi] = a.q1.f[f][gi];
+                    a.q1.f[f][gi] = av[f];
+                    if (a.q1s[0]) a.q1s[f][gi] = narrow(av[f]);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// initial conditions (CSolver_AWS.cpp:199-504)
+// ---------------------------------------------------------------------
+// q1 from rho, p, U, V, W (:207-233); T0 = p/(rho R) (:233).
+__global__ void k_ic(IcArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double r = a.rho0[gi], U = a.U0[gi], V = a.V0[gi], W = a.W0[gi], p = a.p0[gi];
+        a.q1.f[0][gi] = r;
+        a.q1.f[1][gi] = r * U;
+        a.q1.f[2][gi] = r * V;
+        a.q1.f[3][gi] = r * W;
+        a.q1.f[4][gi] = p / (a.gas.gamma - 1.0) + 0.5 * r * (U * U + V * V + W * W);
+        a.T0[gi] = p / (r * a.gas.R);
+    }
+}
+
+// One wall face of the initial state (:258-472): wall velocity into U0,V0,W0
+// and the momenta, Neumann temperature into T0.  One launch per face in the
+// reference's order, so later faces read the temperatures earlier faces set.
+__global__ void k_ic_wall(IcArgs a) {
+    const Geom g = a.g;
+    const int dir = a.face / 2, hi = a.face % 2;
+    const int n1 = dir == 0 ? g.Ny : g.Nx, n2 = dir == 2 ? g.Ny : g.Nz;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n1 * n2) return;
+    int a1 = (int)(idx % n1), a2 = (int)(idx / n1);
+    int Nd = dir == 0 ? g.Nx : dir == 1 ? g.Ny : g.Nz;
+    int fix = hi ? Nd - 1 : 0, sg = hi ? -1 : 1;
+    int i, j, k;
+    if (dir == 0) { i = fix; j = a1; k = a2; }
+    else if (dir == 1) { i = a1; j = fix; k = a2; }
+    else { i = a1; j = a2; k = fix; }
+    const long long nxy = (long long)g.Nx * g.Ny;
+    const long long gi = (long long)k * nxy + (long long)j * g.Nx + i;
+    const long long step = dir == 0 ? 1 : dir == 1 ? g.Nx : nxy;
+    double Tn[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) Tn[m] = a.T0[gi + sg * (m + 1) * step];
+    double Tw = (Tn[0] * 360.0 - Tn[1] * 450.0 + Tn[2] * 400.0 - Tn[3] * 225.0 + Tn[4] * 72.0 - Tn[5] * 10.0) / 147.0;
+    a.T0[gi] = Tw;
+    double r = a.q1.f[0][gi];
+    a.U0[gi] = a.uw[0];
+    a.V0[gi] = a.uw[1];
+    a.W0[gi] = a.uw[2];
+    a.q1.f[1][gi] = dir == 0 ? 0.0 : r * a.uw[0];
+    a.q1.f[2][gi] = dir == 1 ? 0.0 : r * a.uw[1];
+    a.q1.f[3][gi] = dir == 2 ? 0.0 : r * a.uw[2];
+}
+
+// With any wall present the reference recomputes p = rho R T and rhoE from
+// the (wall-modified) U,V,W arrays at every point (:476-484).
+__global__ void k_ic_wall_eos(IcArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double r = a.q1.f[0][gi];
+        double U = a.U0[gi], V = a.V0[gi], W = a.W0[gi];
+        double p = r * a.gas.R * a.T0[gi];
+        a.q1.f[4][gi] = p / (a.gas.gamma - 1.0) + 0.5 * r * (U * U + V * V + W * W);
+    }
+}
+
+// Primitives of q1 for diagnostics: U,V,W,p,T,mu,sos (updateNonConservedData,
+// CSolver_AWS.cpp:1895-1935).
+__global__ void k_primitives(PrimArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double r = a.q.f[0][gi];
+        double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+        double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
+        double T = p / (r * a.gas.R);
+        a.out[0][gi] = U; a.out[1][gi] = V; a.out[2][gi] = W; a.out[3][gi] = p; a.out[4][gi] = T;
+        a.out[5][gi] = a.gas.mu_ref * pow(T, 0.76);
+        a.out[6][gi] = sqrt(a.gas.gamma * p / r);
+    }
+}
+
+// FP32 shadow of an FP64 state (nf fields): out = narrow(q); or, when in is
+// set, the reverse: q = widen(in).
+__global__ void k_shadow(ShadowArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        for (int f = 0; f < a.nf; ++f) {
+            if (a.in[0]) a.q.f[f][gi] = widen(a.in[f][gi]);
+            else a.out[f][gi] = narrow(a.q.f[f][gi]);
+        }
+    }
+}
+
+// Scan a state for non-finite values.
+__global__ void k_nan_scan(CflArgs a) {
+    int bad = 0;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            double v = a.q.f[f][gi];
+            bad |= !(v == v) || isinf(v);
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) *a.nan_flag = 1;
+}
+
+
+// ---------------------------------------------------------------------
+// Taylor-Green diagnostics (CSolver_AWS.cpp:2175-2236): per-block partial
+// sums of enstrophy, 2mu-enstrophy, dissipation, kinetic energy, squared
+// dilatation and mu, reduced in a fixed order on the host.
+// ---------------------------------------------------------------------
+template <typename T>
+__global__ void k_tgv(TgvArgs<T> a) {
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    const double inv_n = 1.0 / (double)a.g.npts;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double Ux = a.dx[0][gi], Vx = a.dx[1][gi], Wx = a.dx[2][gi];
+        double Uy = a.dy[0][gi], Vy = a.dy[1][gi], Wy = a.dy[2][gi];
+        double Uz = a.dz[0][gi], Vz = a.dz[1][gi], Wz = a.dz[2][gi];
+        double r = a.q.f[0][gi];
+        double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+        double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
+        double mu = a.gas.mu_ref * pow(p / (r * a.gas.R), 0.76);
+        double tr = (1.0 / 3.0) * (Ux + Vy + Wz);
+        double S00 = Ux - tr, S11 = Vy - tr, S22 = Wz - tr;
+        double S01 = 0.5 * (Uy + Vx), S02 = 0.5 * (Uz + Wx), S12 = 0.5 * (Vz + Wy);
+        double td = S00 * Ux + S01 * Uy + S02 * Uz + S01 * Vx + S11 * Vy + S12 * Vz + S02 * Wx + S12 * Wy + S22 * Wz;
+        double wx = Wy - Vz, wy = Uz - Wx, wz = Vx - Uy;
+        double om = wx * wx + wy * wy + wz * wz;
+        s[0] += 0.5 * r * om;
+        s[1] += mu * r * om;
+        s[2] += 2.0 * mu * td;
+        s[3] += r * (U * U + V * V + W * W) / 2.0;
+        s[4] += (Ux + Vy + Wz) * (Ux + Vy + Wz) * inv_n;
+        s[5] += mu * inv_n;
+    }
+    __shared__ double red[6][32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        double v = s[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[i][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+        a.out[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+template <typename T>
+cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s) {
+    k_tgv<T><<<blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_tgv<double>(const TgvArgs<double> &, int, cudaStream_t);
+template cudaError_t launch_tgv<float>(const TgvArgs<float> &, int, cudaStream_t);
+
+// ---------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------
+static int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 152 * 16) b = 152 * 16;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+static long long face_points(const Geom &g, int face) {
+    const int dir = face / 2;
+    return dir == 0 ? (long long)g.Ny * g.Nz : dir == 1 ? (long long)g.Nx * g.Nz : (long long)g.Nx * g.Ny;
+}
+
+cudaError_t launch_wall_pre(const BCArgs &a, cudaStream_t s) {
+    k_wall_pre<<<(unsigned)((face_points(a.g, a.face) + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_cfl(const CflArgs &a, cudaStream_t s) {
+    k_cfl<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_nan_scan(const CflArgs &a, cudaStream_t s) {
+    k_nan_scan<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_finalize_dt(const DtArgs &a, cudaStream_t s) {
+    k_finalize_dt<<<1, 1, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_sponge_update(const SpongeArgs &a, cudaStream_t s) {
+    k_sponge_update<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_ic(const IcArgs &a, cudaStream_t s) {
+    k_ic<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_ic_wall(const IcArgs &a, cudaStream_t s) {
+    k_ic_wall<<<(unsigned)((face_points(a.g, a.face) + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_ic_wall_eos(const IcArgs &a, cudaStream_t s) {
+    k_ic_wall_eos<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_primitives(const PrimArgs &a, cudaStream_t s) {
+    k_primitives<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_shadow(const ShadowArgs &a, cudaStream_t s) {
+    k_shadow<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace cs3d

@@ -1,0 +1,973 @@
+// cs3d_sweeps.cu -- the directional sweep kernels of one RK stage, the
+// compact filter and the single-operator kernel (sm_103a).
+//
+// One stage is three fused directional sweeps.  Each sweep kernel takes a
+// pencil tile -- L complete grid lines along the sweep direction -- and runs
+// three phases:
+//
+//   A  load the tile's inputs (batched, several points per thread in
+//      flight), form primitives and fluxes, stage every line-solve input in
+//      shared memory ([position][line] layout);
+//   B  solve: one thread per (line, task); a task is two line solves run
+//      interleaved -- the 1st and 2nd derivative of one field, or the 1st
+//      derivative of two fields -- each a Thomas sweep with precomputed
+//      factors, unrolled in chunks of 4 rows with the next chunk's loads
+//      issued ahead;
+//   C  consume the derivatives point by point.
+//
+//   sweep x : primitives, Euler x-fluxes, 13 x-solves; writes Ux,Vx,Wx,Tx,
+//             mu, mu'(T) and the linear x-part of the five right-hand sides
+//   sweep y : 15 y-solves (incl. the cross derivatives Uxy, Vxy); writes
+//             Uy,Vy,Wy,Ty and adds the linear y-part
+//   sweep z : 16 z-solves (incl. d/dz of Ux+Vy, Wx, Wy), the nonlinear viscous
+//             terms, sponge sources, dt, the wall/sponge increment fix-up and
+//             the RK4 / TVD-RK3 update of the conserved state
+//
+// The reference instead stores ~48 derivative fields and makes ~54 layout
+// transposes per stage (CSolver_AWS.cpp:829-1243).  Lines along y and z are
+// read in place in the XYZ layout: a tile is L consecutive x-columns, so every
+// global access is a contiguous row segment; x-lines are transposed into
+// shared memory on load.
+//
+// T is the work precision: double for the plain form, float for the mixed
+// form.  The conserved state (q1, q2, and qk where kept) is FP64.
+#include <cstdio>
+#include <cmath>
+#include "cs3d_dev.cuh"
+#include "cs3d_kernels.cuh"
+
+namespace cs3d {
+
+// ---------------------------------------------------------------------
+// line solves
+// ---------------------------------------------------------------------
+constexpr int kU = 4;  // rows per unrolled chunk
+
+// The first H and last H rows of the right-hand side, from explicit rows.
+template <typename T, int H>
+__device__ __forceinline__ void boundary_rows(const T *src, int P, const LineOp<T> &op, T pre[2 * H]) {
+    const int N = op.N;
+#pragma unroll
+    for (int b = 0; b < 2 * H; ++b) {
+        const int col = op.boff[b];
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < kTaps; ++k) {
+            int cc = col + k;
+            cc = cc < 0 ? cc + N : (cc >= N ? cc - N : cc);
+            acc = fma(op.btaps[b][k], src[cc * P], acc);
+        }
+        pre[b] = acc * op.scale;
+    }
+}
+
+// Two line solves, A and B, run interleaved by one thread.  Each reads its
+// line from s* (stride P) and writes the uncorrected solution to d*, which may
+// alias s*: the forward pass reads positions beyond the rows it writes, and
+// the boundary rows are formed before any write.  B may also read A's source
+// (1st and 2nd derivative of one field: A in place, B into its own buffer).
+// The Sherman-Morrison factor of a periodic line is formed in FP64 from the
+// line's end values and stored to f* in the work precision.
+template <typename T, int H>
+__device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &oa, T *fa, const T *sb, T *db,
+                                           const LineOp<T> &ob, T *fb, int P) {
+    constexpr int W = 2 * H + 1;
+    const int N = oa.N;
+    T pa[2 * H], pb[2 * H];
+    boundary_rows<T, H>(sa, P, oa, pa);
+    boundary_rows<T, H>(sb, P, ob, pb);
+    T ta[W], tb[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        ta[k] = oa.taps[kMaxH - H + k];
+        tb[k] = ob.taps[kMaxH - H + k];
+    }
+    const T sca = oa.scale, scb = ob.scale;
+    const T *__restrict__ ma = oa.m;
+    const T *__restrict__ mb = ob.m;
+    // window of the first interior row H: positions 0..2H
+    T wa[W], wb[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        wa[k] = k < N ? sa[k * P] : T(0);
+        wb[k] = k < N ? sb[k * P] : T(0);
+    }
+    // rows 0..H-1
+    T ya = pa[0], yb = pb[0];
+    da[0] = ya;
+    db[0] = yb;
+#pragma unroll
+    for (int n = 1; n < H; ++n) {
+        ya = fma(-__ldg(&ma[n]), ya, pa[n]);
+        yb = fma(-__ldg(&mb[n]), yb, pb[n]);
+        da[n * P] = ya;
+        db[n * P] = yb;
+    }
+    // interior rows H..N-H-1 in chunks of kU, next chunk prefetched
+    const int nend = N - H;
+    int n = H;
+    T na[kU], nb[kU], mna[kU], mnb[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+        const int pos = n + H + 1 + j;
+        na[j] = pos < N ? sa[pos * P] : T(0);
+        nb[j] = pos < N ? sb[pos * P] : T(0);
+    }
+    load4(oa.mf, mna);
+    load4(ob.mf, mnb);
+    for (; n + kU <= nend; n += kU) {
+        T ca[kU], cb[kU], mca[kU], mcb[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            ca[j] = na[j]; cb[j] = nb[j]; mca[j] = mna[j]; mcb[j] = mnb[j];
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const int pos = n + kU + H + 1 + j;
+            na[j] = pos < N ? sa[pos * P] : T(0);
+            nb[j] = pos < N ? sb[pos * P] : T(0);
+        }
+        load4(oa.mf + (n + kU - H), mna);
+        load4(ob.mf + (n + kU - H), mnb);
+        T ea[W + kU], eb[W + kU];
+#pragma unroll
+        for (int k = 0; k < W; ++k) { ea[k] = wa[k]; eb[k] = wb[k]; }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) { ea[W + j] = ca[j]; eb[W + j] = cb[j]; }
+        T ra[kU], rb[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            T acc_a = T(0), acc_b = T(0);
+#pragma unroll
+            for (int k = 0; k < W; ++k) {
+                acc_a = fma(ta[k], ea[j + k], acc_a);
+                acc_b = fma(tb[k], eb[j + k], acc_b);
+            }
+            ra[j] = acc_a * sca;
+            rb[j] = acc_b * scb;
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            ya = fma(-mca[j], ya, ra[j]);
+            yb = fma(-mcb[j], yb, rb[j]);
+            da[(n + j) * P] = ya;
+            db[(n + j) * P] = yb;
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) { wa[k] = ea[kU + k]; wb[k] = eb[kU + k]; }
+    }
+    for (; n < nend; ++n) {
+        T acc_a = T(0), acc_b = T(0);
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            acc_a = fma(ta[k], wa[k], acc_a);
+            acc_b = fma(tb[k], wb[k], acc_b);
+        }
+        ya = fma(-__ldg(&ma[n]), ya, acc_a * sca);
+        yb = fma(-__ldg(&mb[n]), yb, acc_b * scb);
+#pragma unroll
+        for (int k = 0; k < W - 1; ++k) { wa[k] = wa[k + 1]; wb[k] = wb[k + 1]; }
+        const int pos = n + H + 1;
+        wa[W - 1] = pos < N ? sa[pos * P] : T(0);
+        wb[W - 1] = pos < N ? sb[pos * P] : T(0);
+        da[n * P] = ya;
+        db[n * P] = yb;
+    }
+    // rows N-H..N-1
+#pragma unroll
+    for (int b = 0; b < H; ++b) {
+        const int r = N - H + b;
+        ya = fma(-__ldg(&ma[r]), ya, pa[H + b]);
+        yb = fma(-__ldg(&mb[r]), yb, pb[H + b]);
+        da[r * P] = ya;
+        db[r * P] = yb;
+    }
+    // back substitution in chunks of kU, next chunk prefetched
+    const T *__restrict__ ca_ = oa.c;
+    const T *__restrict__ cb_ = ob.c;
+    const T *__restrict__ ia = oa.iw;
+    const T *__restrict__ ib = ob.iw;
+    T xa = ya * __ldg(&ia[N - 1]);
+    T xb = yb * __ldg(&ib[N - 1]);
+    da[(N - 1) * P] = xa;
+    db[(N - 1) * P] = xb;
+    const T xla = xa, xlb = xb;
+    n = N - 2;
+    T ya4[kU], yb4[kU], cA[kU], cB[kU], iA[kU], iB[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+        const int r = max(n - j, 0);
+        ya4[j] = da[r * P]; yb4[j] = db[r * P];
+    }
+    load4(oa.cbk, cA); load4(ob.cbk, cB);
+    load4(oa.ibk, iA); load4(ob.ibk, iB);
+    for (; n - kU + 1 >= 0; n -= kU) {
+        T y0a[kU], y0b[kU], c0a[kU], c0b[kU], i0a[kU], i0b[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            y0a[j] = ya4[j]; y0b[j] = yb4[j]; c0a[j] = cA[j]; c0b[j] = cB[j]; i0a[j] = iA[j]; i0b[j] = iB[j];
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const int r = max(n - kU - j, 0);
+            ya4[j] = da[r * P]; yb4[j] = db[r * P];
+        }
+        const int kb = N - 2 - (n - kU);
+        load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+        load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            xa = fma(-c0a[j], xa, y0a[j]) * i0a[j];
+            xb = fma(-c0b[j], xb, y0b[j]) * i0b[j];
+            da[(n - j) * P] = xa;
+            db[(n - j) * P] = xb;
+        }
+    }
+    for (; n >= 0; --n) {
+        xa = fma(-__ldg(&ca_[n]), xa, da[n * P]) * __ldg(&ia[n]);
+        xb = fma(-__ldg(&cb_[n]), xb, db[n * P]) * __ldg(&ib[n]);
+        da[n * P] = xa;
+        db[n * P] = xb;
+    }
+    *fa = oa.periodic ? (T)((to_f64(xa) + oa.bog * to_f64(xla)) * oa.inv_den) : T(0);
+    *fb = ob.periodic ? (T)((to_f64(xb) + ob.bog * to_f64(xlb)) * ob.inv_den) : T(0);
+}
+
+// Corrected value of solution n of a line whose factor is f.
+template <typename T>
+__device__ __forceinline__ T corr(T x, T f, const LineOp<T> &op, int n) {
+    return op.periodic ? fma(-f, __ldg(&op.z[n]), x) : x;
+}
+
+// ---------------------------------------------------------------------
+// tile geometry
+// ---------------------------------------------------------------------
+struct Tile {
+    long long base;   // global index of (line 0, position 0)
+    long long sl, sn; // strides between lines and along a line
+    int nlines;       // valid lines in this tile (<= L)
+    int N;            // line length
+    int ci, cj, ck;   // coordinates of (line 0, position 0)
+};
+
+template <int DIR>
+__device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
+    Tile t;
+    const long long nxy = (long long)g.Nx * g.Ny;
+    if (DIR == 0) {  // x-lines at rows j0.., plane k
+        int j0 = blockIdx.x * L, k = blockIdx.y;
+        t.base = (long long)k * nxy + (long long)j0 * g.Nx;
+        t.sl = g.Nx; t.sn = 1;
+        t.nlines = min(L, g.Ny - j0);
+        t.N = g.Nx;
+        t.ci = 0; t.cj = j0; t.ck = k;
+    } else if (DIR == 1) {  // y-lines at columns i0.., plane k
+        int i0 = blockIdx.x * L, k = blockIdx.y;
+        t.base = (long long)k * nxy + i0;
+        t.sl = 1; t.sn = g.Nx;
+        t.nlines = min(L, g.Nx - i0);
+        t.N = g.Ny;
+        t.ci = i0; t.cj = 0; t.ck = k;
+    } else {  // z-lines at columns i0.., row j
+        int i0 = blockIdx.x * L, j = blockIdx.y;
+        t.base = (long long)j * g.Nx + i0;
+        t.sl = 1; t.sn = nxy;
+        t.nlines = min(L, g.Nx - i0);
+        t.N = g.Nz;
+        t.ci = i0; t.cj = j; t.ck = 0;
+    }
+    return t;
+}
+
+// Point p of a tile: consecutive threads touch consecutive global addresses
+// (position-major for x-lines, line-major otherwise).
+struct Pt {
+    long long gi;  // global index (a valid address even when !ok)
+    int o;         // shared-memory offset
+    int l, n;
+    bool ok;
+};
+
+template <int DIR>
+__device__ __forceinline__ Pt point(const Tile &t, int p, int L, int P) {
+    Pt q;
+    if (DIR == 0) { q.l = p / t.N; q.n = p - q.l * t.N; }
+    else { q.n = p / L; q.l = p - q.n * L; }
+    q.ok = q.l < t.nlines && q.n < t.N;
+    q.gi = q.ok ? t.base + q.l * t.sl + q.n * t.sn : t.base;
+    q.o = q.n * P + q.l;
+    return q;
+}
+
+template <int DIR>
+__device__ __forceinline__ void coords(const Tile &t, int l, int n, int &i, int &j, int &k) {
+    if (DIR == 0) { i = n; j = t.cj + l; k = t.ck; }
+    else if (DIR == 1) { i = t.ci + l; j = n; k = t.ck; }
+    else { i = t.ci + l; j = t.cj; k = n; }
+}
+
+// ---------------------------------------------------------------------
+// shared-memory layout of a tile: per-line factors, then nbuf buffers
+// ---------------------------------------------------------------------
+template <typename T>
+struct Smem {
+    T *buf;
+    T *fact;  // [nbuf][L]
+    int bstride;
+    int P;
+    __device__ T *b(int k) const { return buf + (size_t)k * bstride; }
+};
+
+// Elements between consecutive buffers.  The solve tasks of one warp use
+// buffers two apart (A solves 0,2,4,..; B solves 1,3,5,..), each touching L
+// consecutive lines: a stride s with 2*s*e = L*e (mod 32 banks), e the
+// element size in 4-byte words, places the tasks of a warp on distinct banks.
+__host__ __device__ inline int buf_stride(int N, int P, int L, int e) {
+    const int mod = 16 / e;
+    const int want = (L / 2) % mod;
+    int st = N * P;
+    st += ((want - st % mod) + mod) % mod;
+    return st;
+}
+
+template <typename T>
+__device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<T> s;
+    s.P = P;
+    s.bstride = buf_stride(N, P, L, (int)(sizeof(T) / 4));
+    s.fact = reinterpret_cast<T *>(smem_raw);
+    const int nf = (nbuf * L + 3) & ~3;
+    s.buf = reinterpret_cast<T *>(smem_raw) + nf;
+    return s;
+}
+
+// A task: solve A (src a, dst da, operator oa) and solve B, run together.
+// op: 0 = 1st derivative, 1 = 2nd derivative, 2 = filter.
+struct Task {
+    signed char a, da, oa, b, db, ob;
+};
+
+template <typename T, int H>
+__device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
+                                          const LineOp<T> &op0, const LineOp<T> &op1) {
+    for (int w = threadIdx.x; w < ntask * L; w += blockDim.x) {
+        const int t = w / L, l = w - t * L;
+        if (l >= nlines) continue;
+        const Task tk = tasks[t];
+        const LineOp<T> &oa = tk.oa == 1 ? op1 : op0;
+        const LineOp<T> &ob = tk.ob == 1 ? op1 : op0;
+        solve_pair<T, H>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
+                         sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T get(const Smem<T> &sm, int k, const Pt &p, int L, const LineOp<T> &op) {
+    return corr<T>(sm.b(k)[p.o], sm.fact[k * L + p.l], op, p.n);
+}
+
+// Sherman-Morrison vectors of the 1st and 2nd derivative at position n
+// (zero for wall lines), loaded once per point.
+template <typename T>
+struct Zn {
+    T z1, z2;
+};
+template <typename T>
+__device__ __forceinline__ Zn<T> zn(const LineOp<T> &d1, const LineOp<T> &d2, int n) {
+    Zn<T> z;
+    z.z1 = d1.periodic ? __ldg(&d1.z[n]) : T(0);
+    z.z2 = d2.periodic ? __ldg(&d2.z[n]) : T(0);
+    return z;
+}
+// Corrected solution of buffer k at point p, with z the operator's vector.
+template <typename T>
+__device__ __forceinline__ T gz(const Smem<T> &sm, int k, const Pt &p, int L, T z) {
+    return fma(-sm.fact[k * L + p.l], z, sm.b(k)[p.o]);
+}
+
+// ---------------------------------------------------------------------
+// sweep x
+// ---------------------------------------------------------------------
+enum { XU = 0, XU2, XV, XV2, XW, XW2, XT, XT2, XRU, XF1, XF2, XF3, XF4, XNB };
+__constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}, {XW, XW, 0, XW, XW2, 1},
+                                {XT, XT, 0, XT, XT2, 1}, {XRU, XRU, 0, XF1, XF1, 0},
+                                {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XF4, 0}};
+
+template <typename T>
+struct PrimW {
+    T ru, rv, rw, re, U, V, W, p, Tt;
+};
+
+template <typename T>
+__device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2, T r3, T r4) {
+    PrimW<T> s;
+    s.ru = r1; s.rv = r2; s.rw = r3; s.re = r4;
+    s.U = r1 / r0;
+    s.V = r2 / r0;
+    s.W = r3 / r0;
+    s.p = (T)gp.gm1 * (r4 - T(0.5) * r0 * (s.U * s.U + s.V * s.V + s.W * s.W));
+    s.Tt = s.p / (r0 * (T)gp.R);
+    return s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_x(SweepArgs<T> a) {
+    constexpr int B = sizeof(T) == 4 ? 4 : 2;
+    const int L = a.L, P = a.P;
+    const Tile t = make_tile<0>(a.g, L);
+    const int N = t.N, NL = N * L;
+    Smem<T> sm = smem_layout<T>(XNB, L, P, N);
+    const GasParams gp = a.gas;
+    const T *__restrict__ q0 = a.qs[0];
+    const T *__restrict__ q1 = a.qs[1];
+    const T *__restrict__ q2 = a.qs[2];
+    const T *__restrict__ q3 = a.qs[3];
+    const T *__restrict__ q4 = a.qs[4];
+    // phase A
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        T v[B][5];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<0>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+            v[b][0] = q0[gi]; v[b][1] = q1[gi]; v[b][2] = q2[gi]; v[b][3] = q3[gi]; v[b][4] = q4[gi];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+            const long long gi = pt[b].gi;
+            PrimW<T> s = prim_w<T>(gp, v[b][0], v[b][1], v[b][2], v[b][3], v[b][4]);
+            a.prim[0][gi] = s.U; a.prim[1][gi] = s.V; a.prim[2][gi] = s.W;
+            a.prim[3][gi] = s.p; a.prim[4][gi] = s.Tt;
+            // stage-start primitives: on stage 1, points of SPONGE faces (not
+            // on a wall) use the state before the previous step's sponge
+            // overwrite, which the reference's U,V,W,p,T arrays still hold.
+            PrimW<T> ss = s;
+            if (a.use_backup) {
+                int i, j, k;
+                coords<0>(t, pt[b].l, pt[b].n, i, j, k);
+                const int f = faces_of(a.g, i, j, k);
+                if ((f & a.sponge_kind_faces) && !(f & a.wall_faces))
+                    ss = prim_w<T>(gp, to_work<T>(a.backup.f[0][gi]), to_work<T>(a.backup.f[1][gi]),
+                                   to_work<T>(a.backup.f[2][gi]), to_work<T>(a.backup.f[3][gi]),
+                                   to_work<T>(a.backup.f[4][gi]));
+            }
+            const int o = pt[b].o;
+            sm.b(XU)[o] = ss.U;
+            sm.b(XV)[o] = ss.V;
+            sm.b(XW)[o] = ss.W;
+            sm.b(XT)[o] = ss.Tt;
+            sm.b(XRU)[o] = s.ru;
+            sm.b(XF1)[o] = s.ru * ss.U + ss.p;
+            sm.b(XF2)[o] = s.rv * ss.U;
+            sm.b(XF3)[o] = s.rw * ss.U;
+            sm.b(XF4)[o] = s.re * ss.U + ss.U * ss.p;
+        }
+    }
+    __syncthreads();
+    run_tasks<T, 2>(sm, kTasksX, 7, L, t.nlines, a.d1, a.d2);
+    __syncthreads();
+    // phase C
+    const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        T v[B][4];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<0>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi]; v[b][3] = a.prim[4][gi];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+            const Pt &p = pt[b];
+            const long long gi = p.gi;
+            const Zn<T> zz = zn(a.d1, a.d2, p.n);
+            const T U = v[b][0], V = v[b][1], W = v[b][2], Tt = v[b][3];
+            const T mu = muref * pow(Tt, (T)0.76);
+            const T amu = (T)0.76 * mu / Tt;
+            a.mu[gi] = mu;
+            a.amu[gi] = amu;
+            const T Ux = gz(sm, XU, p, L, zz.z1), Uxx = gz(sm, XU2, p, L, zz.z2);
+            const T Vx = gz(sm, XV, p, L, zz.z1), Vxx = gz(sm, XV2, p, L, zz.z2);
+            const T Wx = gz(sm, XW, p, L, zz.z1), Wxx = gz(sm, XW2, p, L, zz.z2);
+            const T Tx = gz(sm, XT, p, L, zz.z1), Txx = gz(sm, XT2, p, L, zz.z2);
+            const T cex = gz(sm, XRU, p, L, zz.z1);
+            const T f1 = gz(sm, XF1, p, L, zz.z1), f2 = gz(sm, XF2, p, L, zz.z1);
+            const T f3 = gz(sm, XF3, p, L, zz.z1), f4 = gz(sm, XF4, p, L, zz.z1);
+            a.dx[0][gi] = Ux; a.dx[1][gi] = Vx; a.dx[2][gi] = Wx; a.dx[3][gi] = Tx;
+            a.R[0][gi] = -cex;
+            a.R[1][gi] = mu * (c43 * Uxx) - f1;
+            a.R[2][gi] = mu * Vxx - f2;
+            a.R[3][gi] = mu * Wxx - f3;
+            a.R[4][gi] = cpPr * mu * Txx + mu * (U * (c43 * Uxx) + V * Vxx + W * Wxx) - f4;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// sweep y
+// ---------------------------------------------------------------------
+enum { YU = 0, YU2, YV, YV2, YW, YW2, YT, YT2, YUX, YVX, YRV, YF1, YF2, YF3, YF4, YNB };
+__constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}, {YW, YW, 0, YW, YW2, 1},
+                                {YT, YT, 0, YT, YT2, 1}, {YUX, YUX, 0, YVX, YVX, 0},
+                                {YRV, YRV, 0, YF1, YF1, 0}, {YF2, YF2, 0, YF3, YF3, 0},
+                                {YF4, YF4, 0, YF4, YF4, 0}};
+
+template <typename T>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_y(SweepArgs<T> a) {
+    constexpr int B = sizeof(T) == 4 ? 4 : 2;
+    const int L = a.L, P = a.P;
+    const Tile t = make_tile<1>(a.g, L);
+    const int N = t.N, NL = N * L;
+    Smem<T> sm = smem_layout<T>(YNB, L, P, N);
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        T v[B][11];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<1>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) v[b][f] = a.qs[f + 1][gi];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.prim[f][gi];
+            v[b][9] = a.dx[0][gi];
+            v[b][10] = a.dx[1][gi];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+            const int o = pt[b].o;
+            const T ru = v[b][0], rv = v[b][1], rw = v[b][2], re = v[b][3];
+            const T U = v[b][4], V = v[b][5], W = v[b][6], pp = v[b][7], Tt = v[b][8];
+            sm.b(YU)[o] = U;
+            sm.b(YV)[o] = V;
+            sm.b(YW)[o] = W;
+            sm.b(YT)[o] = Tt;
+            sm.b(YUX)[o] = v[b][9];
+            sm.b(YVX)[o] = v[b][10];
+            sm.b(YRV)[o] = rv;
+            sm.b(YF1)[o] = ru * V;
+            sm.b(YF2)[o] = rv * V + pp;
+            sm.b(YF3)[o] = rw * V;
+            sm.b(YF4)[o] = re * V + V * pp;
+        }
+    }
+    __syncthreads();
+    run_tasks<T, 2>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
+    __syncthreads();
+    const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        T v[B][9];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<1>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi];
+            v[b][3] = a.mu[gi];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.R[f][gi];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+            const Pt &p = pt[b];
+            const long long gi = p.gi;
+            const Zn<T> zz = zn(a.d1, a.d2, p.n);
+            const T U = v[b][0], V = v[b][1], W = v[b][2], mu = v[b][3];
+            const T Uy = gz(sm, YU, p, L, zz.z1), Uyy = gz(sm, YU2, p, L, zz.z2);
+            const T Vy = gz(sm, YV, p, L, zz.z1), Vyy = gz(sm, YV2, p, L, zz.z2);
+            const T Wy = gz(sm, YW, p, L, zz.z1), Wyy = gz(sm, YW2, p, L, zz.z2);
+            const T Ty = gz(sm, YT, p, L, zz.z1), Tyy = gz(sm, YT2, p, L, zz.z2);
+            const T Uxy = gz(sm, YUX, p, L, zz.z1), Vxy = gz(sm, YVX, p, L, zz.z1);
+            const T cey = gz(sm, YRV, p, L, zz.z1);
+            const T f1 = gz(sm, YF1, p, L, zz.z1), f2 = gz(sm, YF2, p, L, zz.z1);
+            const T f3 = gz(sm, YF3, p, L, zz.z1), f4 = gz(sm, YF4, p, L, zz.z1);
+            a.dy[0][gi] = Uy; a.dy[1][gi] = Vy; a.dy[2][gi] = Wy; a.dy[3][gi] = Ty;
+            int i, j, k;
+            coords<1>(t, p.l, p.n, i, j, k);
+            const int wd = a.wall_faces ? wall_dir(faces_of(a.g, i, j, k) & a.wall_faces) : -1;
+            if (wd == 1) a.R[0][gi] = -cey;
+            else if (wd < 0) a.R[0][gi] = v[b][4] - cey;
+            a.R[1][gi] = v[b][5] + (mu * (Uyy + c13 * Vxy) - f1);
+            a.R[2][gi] = v[b][6] + (mu * (c43 * Vyy + c13 * Uxy) - f2);
+            a.R[3][gi] = v[b][7] + (mu * Wyy - f3);
+            a.R[4][gi] = v[b][8] +
+                         (cpPr * mu * Tyy + mu * (U * Uyy + V * (c43 * Vyy) + W * Wyy + c13 * (U * Vxy + V * Uxy)) - f4);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// sweep z + right-hand side + RK update
+// ---------------------------------------------------------------------
+enum { ZU = 0, ZU2, ZV, ZV2, ZW, ZW2, ZT, ZT2, ZS, ZWX, ZWY, ZRW, ZF1, ZF2, ZF3, ZF4, ZNB };
+__constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}, {ZW, ZW, 0, ZW, ZW2, 1},
+                                {ZT, ZT, 0, ZT, ZT2, 1}, {ZS, ZS, 0, ZWX, ZWX, 0},
+                                {ZWY, ZWY, 0, ZRW, ZRW, 0}, {ZF1, ZF1, 0, ZF2, ZF2, 0},
+                                {ZF3, ZF3, 0, ZF4, ZF4, 0}};
+
+template <typename T>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepArgs<T> a) {
+    constexpr int BA = sizeof(T) == 4 ? 4 : 2;
+    constexpr int BC = 2;
+    const int L = a.L, P = a.P;
+    const Tile t = make_tile<2>(a.g, L);
+    const int N = t.N, NL = N * L;
+    Smem<T> sm = smem_layout<T>(ZNB, L, P, N);
+    for (int p0 = threadIdx.x; p0 < NL; p0 += BA * blockDim.x) {
+        Pt pt[BA];
+        T v[BA][13];
+#pragma unroll
+        for (int b = 0; b < BA; ++b) {
+            pt[b] = point<2>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) v[b][f] = a.qs[f + 1][gi];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.prim[f][gi];
+            v[b][9] = a.dx[0][gi];
+            v[b][10] = a.dy[1][gi];
+            v[b][11] = a.dx[2][gi];
+            v[b][12] = a.dy[2][gi];
+        }
+#pragma unroll
+        for (int b = 0; b < BA; ++b) {
+            if (!pt[b].ok) continue;
+            const int o = pt[b].o;
+            const T ru = v[b][0], rv = v[b][1], rw = v[b][2], re = v[b][3];
+            const T U = v[b][4], V = v[b][5], W = v[b][6], pp = v[b][7], Tt = v[b][8];
+            sm.b(ZU)[o] = U;
+            sm.b(ZV)[o] = V;
+            sm.b(ZW)[o] = W;
+            sm.b(ZT)[o] = Tt;
+            sm.b(ZS)[o] = v[b][9] + v[b][10];
+            sm.b(ZWX)[o] = v[b][11];
+            sm.b(ZWY)[o] = v[b][12];
+            sm.b(ZRW)[o] = rw;
+            sm.b(ZF1)[o] = ru * W;
+            sm.b(ZF2)[o] = rv * W;
+            sm.b(ZF3)[o] = rw * W + pp;
+            sm.b(ZF4)[o] = re * W + W * pp;
+        }
+    }
+    __syncthreads();
+    run_tasks<T, 2>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
+    __syncthreads();
+    const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), c23 = T(2.0 / 3.0), cpPr = (T)a.gas.cpPr;
+    const double dt = *a.dt;
+    const T dtw = (T)dt;
+    const int st = a.rk_step;
+    const bool tvd = a.rk == 1;
+    // which state arrays the update reads (uniform over the launch):
+    //   qa = q1 (RK4 stage 1, all TVD-RK3 stages) or q2 (RK4 stages 2-4)
+    //   qb = q1 for the FP64 RK4 qk update on stages 2-3, or the FP64 qk of
+    //        TVD-RK3 stages 2-3
+    const bool use_q1a = tvd || st == 1;
+    const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
+    const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
+    const bool need_qs = a.sponge || (a.mixed_rk4 && st == 1);
+    for (int p0 = threadIdx.x; p0 < NL; p0 += BC * blockDim.x) {
+        Pt pt[BC];
+        T v[BC][18];
+        double qa[BC][5], qb[BC][5], sav[BC][5], sgv[BC];
+        T qsv[BC][5];
+        float q1f[BC][5];
+        // all global loads of the batch first: no store can alias them
+#pragma unroll
+        for (int b = 0; b < BC; ++b) {
+            pt[b] = point<2>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi];
+            v[b][3] = a.mu[gi]; v[b][4] = a.amu[gi];
+#pragma unroll
+            for (int f = 0; f < 4; ++f) { v[b][5 + f] = a.dx[f][gi]; v[b][9 + f] = a.dy[f][gi]; }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                v[b][13 + f] = a.R[f][gi];
+                qa[b][f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
+                qb[b][f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
+                q1f[b][f] = need_q1s ? a.q1s[f][gi] : 0.f;
+                qsv[b][f] = need_qs ? a.qs[f][gi] : T(0);
+                sav[b][f] = a.sponge ? a.savg.f[f][gi] : 0.0;
+            }
+            sgv[b] = a.sponge ? a.sigma[gi] : 0.0;
+        }
+#pragma unroll
+        for (int b = 0; b < BC; ++b) {
+            if (!pt[b].ok) continue;
+            const Pt &p = pt[b];
+            const long long gi = p.gi;
+            const Zn<T> zz = zn(a.d1, a.d2, p.n);
+            const T U = v[b][0], V = v[b][1], W = v[b][2], mu = v[b][3], amu = v[b][4];
+            const T Ux = v[b][5], Vx = v[b][6], Wx = v[b][7], Tx = v[b][8];
+            const T Uy = v[b][9], Vy = v[b][10], Wy = v[b][11], Ty = v[b][12];
+            const T Uz = gz(sm, ZU, p, L, zz.z1), Uzz = gz(sm, ZU2, p, L, zz.z2);
+            const T Vz = gz(sm, ZV, p, L, zz.z1), Vzz = gz(sm, ZV2, p, L, zz.z2);
+            const T Wz = gz(sm, ZW, p, L, zz.z1), Wzz = gz(sm, ZW2, p, L, zz.z2);
+            const T Tz = gz(sm, ZT, p, L, zz.z1), Tzz = gz(sm, ZT2, p, L, zz.z2);
+            const T S = gz(sm, ZS, p, L, zz.z1);  // Uxz + Vyz
+            const T Wxz = gz(sm, ZWX, p, L, zz.z1), Wyz = gz(sm, ZWY, p, L, zz.z1);
+            const T cez = gz(sm, ZRW, p, L, zz.z1);
+            const T f1 = gz(sm, ZF1, p, L, zz.z1), f2 = gz(sm, ZF2, p, L, zz.z1);
+            const T f3 = gz(sm, ZF3, p, L, zz.z1), f4 = gz(sm, ZF4, p, L, zz.z1);
+            T src[5] = {T(0), T(0), T(0), T(0), T(0)};
+            if (a.sponge) {
+                const T sg = to_work<T>(sgv[b]);
+#pragma unroll
+                for (int f = 0; f < 5; ++f) src[f] = sg * (to_work<T>(sav[b][f]) - qsv[b][f]);
+            }
+            const T MuX = amu * Tx, MuY = amu * Ty, MuZ = amu * Tz;
+            T R[5];
+            R[0] = v[b][13];
+            R[1] = v[b][14] + mu * (Uzz + c13 * Wxz) - f1 + c43 * MuX * (Ux - T(0.5) * Vy - T(0.5) * Wz) +
+                   MuY * (Uy + Vx) + MuZ * (Wx + Uz) + src[1];
+            R[2] = v[b][15] + mu * (Vzz + c13 * Wyz) - f2 + c43 * MuY * (Vy - T(0.5) * Ux - T(0.5) * Wz) +
+                   MuX * (Uy + Vx) + MuZ * (Wy + Vz) + src[2];
+            R[3] = v[b][16] + mu * (c43 * Wzz + c13 * S) - f3 + c43 * MuZ * (Wz - T(0.5) * Ux - T(0.5) * Vy) +
+                   MuX * (Wx + Uz) + MuY * (Wy + Vz) + src[3];
+            const T q2s = Ux * Ux + Vy * Vy + Wz * Wz;
+            const T sq = Uy * Uy + Uz * Uz + Vx * Vx + Vz * Vz + Wx * Wx + Wy * Wy;
+            const T cr = Ux * Vy + Ux * Wz + Vy * Wz;
+            const T sh = Uy * Vx + Uz * Wx + Vz * Wy;
+            const T v1 = mu * (U * Uzz + V * Vzz + W * (c43 * Wzz) + c13 * (U * Wxz + V * Wyz + W * S) + c43 * q2s +
+                               sq - c43 * cr + T(2.0) * sh);
+            const T v2 = c43 * (U * MuX * Ux + V * MuY * Vy + W * MuZ * Wz) - c23 * U * MuX * (Vy + Wz) -
+                         c23 * V * MuY * (Ux + Wz) - c23 * W * MuZ * (Ux + Vy) + U * MuY * (Uy + Vx) +
+                         U * MuZ * (Uz + Wx) + V * MuX * (Uy + Vx) + V * MuZ * (Vz + Wy) + W * MuX * (Uz + Wx) +
+                         W * MuY * (Vz + Wy);
+            R[4] = v[b][17] + cpPr * (MuX * Tx + MuY * Ty + MuZ * Tz + mu * Tzz) + v1 + v2 - f4 + T(2.0) * src[4];
+            // continuity and the post-step boundary fix-up (CSolver_AWS.cpp:1506-1679)
+            int i, j, k;
+            coords<2>(t, p.l, p.n, i, j, k);
+            const int fc = faces_of(a.g, i, j, k);
+            const int wd = a.wall_faces ? wall_dir(fc & a.wall_faces) : -1;
+            if (wd == 2) R[0] = -cez;
+            else if (wd < 0) R[0] = R[0] - cez + src[0];
+            const bool zero_all = (fc & a.sponge_kind_faces) != 0;
+            const bool zero_mom = wd >= 0;
+            // results of the point: stores only from here on
+            if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
+                a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
+            }
+            if (sizeof(T) == 8) {
+                // plain form: dq = dt * RHS and the reference's RK update in FP64
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    double d = dt * (double)R[f];
+                    if (zero_all || (f > 0 && zero_mom)) d = 0.0;
+                    if (a.dq_out[0]) a.dq_out[f][gi] = d;
+                    if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
+                        if (st == 1) a.qk.f[f][gi] = qa[b][f] + d;
+                        else if (st == 2) a.qk.f[f][gi] = 0.75 * qa[b][f] + 0.25 * qb[b][f] + 0.25 * d;
+                        else a.q2.f[f][gi] = (1.0 / 3.0) * qa[b][f] + (2.0 / 3.0) * qb[b][f] + (2.0 / 3.0) * d;
+                    } else {    // RK4 (RK4.hpp:35-118); qa = q1 (stage 1) or q2
+                        const double ca = (st == 1 || st == 4) ? (1.0 / 6.0) : (1.0 / 3.0);
+                        const double cb = (st == 3) ? 1.0 : 0.5;
+                        a.q2.f[f][gi] = qa[b][f] + ca * d;
+                        if (st == 1) a.qk.f[f][gi] = qa[b][f] + cb * d;
+                        else if (st < 4) a.qk.f[f][gi] = qb[b][f] + cb * d;
+                    }
+                }
+            } else {
+                // mixed form: the increment dq = dt*RHS in FP32; the conserved
+                // state accumulates it in FP64
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    T d = dtw * R[f];
+                    if (zero_all || (f > 0 && zero_mom)) d = T(0);
+                    if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
+                    if (tvd) {
+                        const double dd = to_f64(d);
+                        double nv;
+                        if (st == 1) { nv = qa[b][f] + dd; a.qk.f[f][gi] = nv; }
+                        else if (st == 2) { nv = 0.75 * qa[b][f] + 0.25 * qb[b][f] + 0.25 * dd; a.qk.f[f][gi] = nv; }
+                        else { nv = (1.0 / 3.0) * qa[b][f] + (2.0 / 3.0) * qb[b][f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
+                        if (a.shadow_target != SHADOW_NONE) a.shadow_out[f][gi] = narrow(nv);
+                    } else {
+                        const T ca = (st == 1 || st == 4) ? T(1.0 / 6.0) : T(1.0 / 3.0);
+                        const T cb = (st == 3) ? T(1.0) : T(0.5);
+                        const double q2n = qa[b][f] + to_f64(ca * d);
+                        a.q2.f[f][gi] = q2n;
+                        if (st < 4) {
+                            // the next stage input qk = q1 + cb*dq, kept as an FP32 shadow
+                            const T q1s = st == 1 ? qsv[b][f] : (T)q1f[b][f];
+                            a.shadow_out[f][gi] = fma(cb, d, q1s);
+                        } else if (a.shadow_target == SHADOW_Q2) {
+                            a.shadow_out[f][gi] = narrow(q2n);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// compact filter, one direction, five fields (Filter.cpp:98-171)
+// ---------------------------------------------------------------------
+// Plain form: FP64 in, FP64 out.  Mixed form: the first pass reads FP64 q2
+// minus a per-field reference value (the field's initial mean, so the FP32
+// numbers are fluctuations), the middle pass works in FP32, and the last pass
+// writes q1 = q2 + (filtered - unfiltered) in FP64 plus q1's FP32 shadow.
+__constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
+
+template <typename T, int DIR>
+__global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
+    constexpr int B = 2;
+    const int L = a.L, P = a.P;
+    const Tile t = make_tile<DIR>(a.g, L);
+    const int N = t.N, NL = N * L;
+    Smem<T> sm = smem_layout<T>(5, L, P, N);
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        T v[B][5];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P);
+            const long long gi = pt[b].gi;
+#pragma unroll
+            for (int f = 0; f < 5; ++f)
+                v[b][f] = a.src64.f[f] ? to_work<T>(a.src64.f[f][gi] - a.ref[f]) : a.src32[f][gi];
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) sm.b(f)[pt[b].o] = v[b][f];
+        }
+    }
+    __syncthreads();
+    run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
+    __syncthreads();
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        Pt pt[B];
+        double q[B][5];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P);
+#pragma unroll
+            for (int f = 0; f < 5; ++f) q[b][f] = a.delta_from.f[f] ? a.delta_from.f[f][pt[b].gi] : 0.0;
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            if (!pt[b].ok) continue;
+            const long long gi = pt[b].gi;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                const T v = get(sm, f, pt[b], L, a.op);
+                if (a.dst64.f[f]) {
+                    double nv;
+                    if (a.delta_from.f[f]) {
+                        const T v0 = to_work<T>(q[b][f] - a.ref[f]);
+                        nv = q[b][f] + to_f64(v - v0);
+                    } else {
+                        nv = to_f64(v) + a.ref[f];
+                    }
+                    a.dst64.f[f][gi] = nv;
+                    if (a.shadow_out[0]) a.shadow_out[f][gi] = narrow(nv);
+                } else {
+                    a.dst32[f][gi] = v;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// single operator on contiguous lines (Derivatives::calc1stDerivField etc.)
+// ---------------------------------------------------------------------
+__constant__ Task kTaskLone[1] = {{0, 0, 0, 0, 0, 0}};
+
+template <int H>
+__global__ void __launch_bounds__(128) k_line_op(LineOpArgs a) {
+    const int L = a.L, N = a.op.N, P = a.P;
+    const long long l0 = (long long)blockIdx.x * L;
+    const int nl = (int)min((long long)L, a.nlines - l0);
+    Smem<double> sm = smem_layout<double>(1, L, P, N);
+    for (int p = threadIdx.x; p < N * L; p += blockDim.x) {
+        const int l = p / N, n = p - l * N;
+        if (l >= nl) continue;
+        sm.b(0)[n * P + l] = a.in[(l0 + l) * N + n];
+    }
+    __syncthreads();
+    run_tasks<double, H>(sm, kTaskLone, 1, L, nl, a.op, a.op);
+    __syncthreads();
+    for (int p = threadIdx.x; p < N * L; p += blockDim.x) {
+        Pt q;
+        q.l = p / N;
+        q.n = p - q.l * N;
+        if (q.l >= nl) continue;
+        q.o = q.n * P + q.l;
+        a.out[(l0 + q.l) * N + q.n] = get(sm, 0, q, L, a.op);
+    }
+}
+
+// ---------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------
+template <typename T>
+static size_t tile_smem(int nbuf, int L, int P, int N) {
+    const int nf = (nbuf * L + 3) & ~3;
+    return sizeof(T) * ((size_t)nf + (size_t)nbuf * buf_stride(N, P, L, (int)(sizeof(T) / 4)));
+}
+
+size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
+    return prec_bytes == 8 ? tile_smem<double>(nbuf, L, P, N) : tile_smem<float>(nbuf, L, P, N);
+}
+int sweep_nbuf(int dir) { return dir == 0 ? XNB : dir == 1 ? YNB : ZNB; }
+int sweep_ntask(int dir) { return dir == 0 ? 7 : 8; }
+int filter_ntask() { return 3; }
+
+template <typename K, typename A>
+static cudaError_t launch_tile_kernel(K kernel, const A &a, dim3 grid, size_t sm, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, a.threads, sm, s>>>(a);
+    return cudaGetLastError();
+}
+
+static dim3 tile_grid(int dir, const Geom &g, int L) {
+    if (dir == 0) return dim3((g.Ny + L - 1) / L, g.Nz);
+    if (dir == 1) return dim3((g.Nx + L - 1) / L, g.Nz);
+    return dim3((g.Nx + L - 1) / L, g.Ny);
+}
+
+template <typename T>
+cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s) {
+    const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
+    const size_t sm = tile_smem<T>(sweep_nbuf(dir), a.L, a.P, N);
+    const dim3 grid = tile_grid(dir, a.g, a.L);
+    if (dir == 0) return launch_tile_kernel(k_sweep_x<T>, a, grid, sm, s);
+    if (dir == 1) return launch_tile_kernel(k_sweep_y<T>, a, grid, sm, s);
+    return launch_tile_kernel(k_sweep_z<T>, a, grid, sm, s);
+}
+
+template <typename T>
+cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s) {
+    const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
+    const size_t sm = tile_smem<T>(5, a.L, a.P, N);
+    const dim3 grid = tile_grid(dir, a.g, a.L);
+    if (dir == 0) return launch_tile_kernel(k_filter<T, 0>, a, grid, sm, s);
+    if (dir == 1) return launch_tile_kernel(k_filter<T, 1>, a, grid, sm, s);
+    return launch_tile_kernel(k_filter<T, 2>, a, grid, sm, s);
+}
+
+cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s) {
+    const size_t sm = tile_smem<double>(1, a.L, a.P, a.op.N);
+    const dim3 grid((unsigned)((a.nlines + a.L - 1) / a.L));
+    if (a.op.H == 4) return launch_tile_kernel(k_line_op<4>, a, grid, sm, s);
+    return launch_tile_kernel(k_line_op<2>, a, grid, sm, s);
+}
+
+template cudaError_t launch_sweep<double>(int, const SweepArgs<double> &, cudaStream_t);
+template cudaError_t launch_sweep<float>(int, const SweepArgs<float> &, cudaStream_t);
+template cudaError_t launch_filter<double>(int, const FilterArgs<double> &, cudaStream_t);
+template cudaError_t launch_filter<float>(int, const FilterArgs<float> &, cudaStream_t);
+
+}  // namespace cs3d
