@@ -26,7 +26,7 @@ from ._abi import (  # noqa: F401  (re-exported constants)
     FP32_MIXED, SPONGE_REFERENCE, SPONGE_BANDS)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libcs3d_gb300.so")
+LIB_PATH = os.environ.get("CS3D_LIB_PATH") or os.path.join(HERE, "libcs3d_gb300.so")
 
 OPT_STORE_INCREMENTS = 1
 OPT_STORE_DIAGNOSTICS = 2

@@ -223,9 +223,10 @@ int upload_op(const HostOp &h, DevOp<T> &d, cudaStream_t s) {
     o.mf = d.mem + 4 * S;
     o.cbk = d.mem + 5 * S;
     o.ibk = d.mem + 6 * S;
-    for (int k = 0; k < kTaps; k++) o.taps[k] = (T)h.taps[k];
+    // the 1/h or 1/h^2 of the right-hand side is folded into the taps
+    for (int k = 0; k < kTaps; k++) o.taps[k] = (T)(h.taps[k] * h.scale);
     for (int b = 0; b < 2 * kMaxH; b++) {
-        for (int k = 0; k < kTaps; k++) o.btaps[b][k] = (T)h.btaps[b][k];
+        for (int k = 0; k < kTaps; k++) o.btaps[b][k] = (T)(h.btaps[b][k] * h.scale);
         o.boff[b] = h.boff[b];
     }
     o.scale = (T)h.scale;
@@ -362,6 +363,12 @@ static int dalloc(cs3d_handle *h, void **p, size_t bytes) {
     return CS3D_OK;
 }
 
+static int ilog2(int v) {
+    int r = 0;
+    while ((1 << (r + 1)) <= v) ++r;
+    return r;
+}
+
 static int face_band_flags(const cs3d_config *c, int *wall, int *spk) {
     *wall = 0;
     *spk = 0;
@@ -399,6 +406,10 @@ static int check_config(const cs3d_config *c) {
         // periodic filter stencil spans 9 points
         if (Nd[d] < 8) return fail(CS3D_ERR_SHAPE, "N[%d]=%d: every direction needs at least 8 points", d, Nd[d]);
         if (Nd[d] > 4096) return fail(CS3D_ERR_SHAPE, "N[%d]=%d exceeds 4096 points per line", d, Nd[d]);
+    }
+    if ((long long)c->Nx * c->Ny * c->Nz >= (1ll << 31))
+        return fail(CS3D_ERR_SHAPE, "Nx*Ny*Nz must stay below 2^31 points (32-bit indexing)");
+    for (int d = 0; d < 3; d++) {
         if (!(Ld[d] > 0.0)) return fail(CS3D_ERR_ARG, "L[%d] must be positive", d);
     }
     for (int f = 0; f < 6; f++)
@@ -415,12 +426,12 @@ static int check_config(const cs3d_config *c) {
 }
 
 // Tile width: the widest power of two (<= 32 lines) whose shared memory
-// stays within the per-block budget: 40 KB in the mixed form (five blocks per
-// SM, so one block's loads overlap another's solves), 72 KB in the plain form
-// (FP64-throughput bound; three blocks per SM keep the FP64 pipe busy).
-// CS3D_SMEM_BUDGET_KB overrides the budget.
+// stays within the per-block budget of 72 KB, three blocks per SM.  For the
+// y and z sweeps of the mixed form at N = 128 this gives 8 lines: every
+// global access is then a full 32-byte sector, which measured faster than
+// narrower tiles with more blocks per SM.  CS3D_SMEM_BUDGET_KB overrides it.
 static int pick_L(size_t tb, int nbuf, int N, int pitch_plus) {
-    size_t budget = (tb == 4 ? 40 : 72) * 1024;
+    size_t budget = 72 * 1024;
     if (const char *e = getenv("CS3D_SMEM_BUDGET_KB")) {
         long v = strtol(e, nullptr, 10);
         if (v >= 8 && v <= 220) budget = (size_t)v * 1024;
@@ -554,6 +565,10 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
     h->threads = 128;
+    if (const char *e = getenv("CS3D_THREADS")) {
+        long v = strtol(e, nullptr, 10);
+        if (v == 64 || v == 128) h->threads = (int)v;
+    }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
     return CS3D_OK;
@@ -772,6 +787,8 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.savg = h->savg;
     for (int d = 0; d < 3; d++) {
         a.L = h->L[d];
+        a.lgL = ilog2(h->L[d]);
+        a.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
         a.P = h->L[d] + (d == 0 ? 1 : 0);
         if (sizeof(T) == 8) {
             a.d1 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][0].op);
@@ -798,6 +815,8 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                 FilterArgs<T> fa{};
                 fa.g = h->g;
                 fa.L = h->Lf[d];
+                fa.lgL = ilog2(h->Lf[d]);
+                fa.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
                 fa.P = h->Lf[d] + (d == 0 ? 1 : 0);
                 fa.threads = h->threads;
                 if (sizeof(T) == 8) fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][2].op);

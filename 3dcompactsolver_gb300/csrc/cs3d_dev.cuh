@@ -57,6 +57,22 @@ struct Q5 {
     double *f[5];
 };
 
+// Division by a fixed d > 0 of numerators below 2^31:
+// p / d = (umulhi(p, mul) + p) >> sh  (Granlund-Montgomery, round-up form).
+struct FastDiv {
+    unsigned mul;
+    int sh;
+};
+
+inline FastDiv make_fastdiv(unsigned d) {
+    FastDiv f;
+    int sh = 0;
+    while ((1ull << sh) < d) ++sh;
+    f.sh = sh;
+    f.mul = (unsigned)((((1ull << 32) * ((1ull << sh) - d)) / d) + 1ull);
+    return f;
+}
+
 // Grid geometry.
 struct Geom {
     int Nx, Ny, Nz;

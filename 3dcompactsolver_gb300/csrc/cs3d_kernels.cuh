@@ -19,7 +19,9 @@ enum ShadowTarget { SHADOW_NONE = 0, SHADOW_QK = 1, SHADOW_Q2 = 2 };
 template <typename T>
 struct SweepArgs {
     Geom g;
-    int L;          // lines per tile
+    int L;          // lines per tile (a power of two)
+    int lgL;        // log2(L)
+    FastDiv divN;   // division by the line length (x sweep)
     int P;          // shared-memory pitch between positions of a line
     int threads;    // threads per block
     LineOp<T> d1, d2;
@@ -54,7 +56,8 @@ struct SweepArgs {
 template <typename T>
 struct FilterArgs {
     Geom g;
-    int L, P, threads;
+    int L, lgL, P, threads;
+    FastDiv divN;
     LineOp<T> op;
     Q5 src64;          // FP64 source (or null pointers)
     T *src32[5];       // work-precision source

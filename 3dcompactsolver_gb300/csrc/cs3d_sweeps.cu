@@ -36,12 +36,22 @@
 #include "cs3d_dev.cuh"
 #include "cs3d_kernels.cuh"
 
+#ifndef CS3D_ZBC
+#define CS3D_ZBC 2     // points per thread in flight in the z sweep's consume phase
+#endif
+#ifndef CS3D_MINB
+#define CS3D_MINB 3    // resident blocks per SM the mixed-form sweeps are compiled for
+#endif
+
 namespace cs3d {
 
 // ---------------------------------------------------------------------
 // line solves
 // ---------------------------------------------------------------------
 constexpr int kU = 4;  // rows per unrolled chunk
+// Rows of padding after each line buffer in shared memory, so that the
+// chunked forward pass may read ahead past the line's end without a test.
+constexpr int kPad = 2 * kU + kMaxH + 2;
 
 // The first H and last H rows of the right-hand side, from explicit rows.
 template <typename T, int H>
@@ -57,7 +67,7 @@ __device__ __forceinline__ void boundary_rows(const T *src, int P, const LineOp<
             cc = cc < 0 ? cc + N : (cc >= N ? cc - N : cc);
             acc = fma(op.btaps[b][k], src[cc * P], acc);
         }
-        pre[b] = acc * op.scale;
+        pre[b] = acc;
     }
 }
 
@@ -82,15 +92,14 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
         ta[k] = oa.taps[kMaxH - H + k];
         tb[k] = ob.taps[kMaxH - H + k];
     }
-    const T sca = oa.scale, scb = ob.scale;
     const T *__restrict__ ma = oa.m;
     const T *__restrict__ mb = ob.m;
     // window of the first interior row H: positions 0..2H
     T wa[W], wb[W];
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-        wa[k] = k < N ? sa[k * P] : T(0);
-        wb[k] = k < N ? sb[k * P] : T(0);
+        wa[k] = sa[k * P];
+        wb[k] = sb[k * P];
     }
     // rows 0..H-1
     T ya = pa[0], yb = pb[0];
@@ -110,11 +119,12 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
 #pragma unroll
     for (int j = 0; j < kU; ++j) {
         const int pos = n + H + 1 + j;
-        na[j] = pos < N ? sa[pos * P] : T(0);
-        nb[j] = pos < N ? sb[pos * P] : T(0);
+        na[j] = sa[pos * P];
+        nb[j] = sb[pos * P];
     }
     load4(oa.mf, mna);
     load4(ob.mf, mnb);
+#pragma unroll 2
     for (; n + kU <= nend; n += kU) {
         T ca[kU], cb[kU], mca[kU], mcb[kU];
 #pragma unroll
@@ -124,8 +134,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
             const int pos = n + kU + H + 1 + j;
-            na[j] = pos < N ? sa[pos * P] : T(0);
-            nb[j] = pos < N ? sb[pos * P] : T(0);
+            na[j] = sa[pos * P];
+            nb[j] = sb[pos * P];
         }
         load4(oa.mf + (n + kU - H), mna);
         load4(ob.mf + (n + kU - H), mnb);
@@ -143,8 +153,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
                 acc_a = fma(ta[k], ea[j + k], acc_a);
                 acc_b = fma(tb[k], eb[j + k], acc_b);
             }
-            ra[j] = acc_a * sca;
-            rb[j] = acc_b * scb;
+            ra[j] = acc_a;
+            rb[j] = acc_b;
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
@@ -163,8 +173,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
             acc_a = fma(ta[k], wa[k], acc_a);
             acc_b = fma(tb[k], wb[k], acc_b);
         }
-        ya = fma(-__ldg(&ma[n]), ya, acc_a * sca);
-        yb = fma(-__ldg(&mb[n]), yb, acc_b * scb);
+        ya = fma(-__ldg(&ma[n]), ya, acc_a);
+        yb = fma(-__ldg(&mb[n]), yb, acc_b);
 #pragma unroll
         for (int k = 0; k < W - 1; ++k) { wa[k] = wa[k + 1]; wb[k] = wb[k + 1]; }
         const int pos = n + H + 1;
@@ -201,6 +211,7 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     }
     load4(oa.cbk, cA); load4(ob.cbk, cB);
     load4(oa.ibk, iA); load4(ob.ibk, iB);
+#pragma unroll 2
     for (; n - kU + 1 >= 0; n -= kU) {
         T y0a[kU], y0b[kU], c0a[kU], c0b[kU], i0a[kU], i0b[kU];
 #pragma unroll
@@ -243,8 +254,8 @@ __device__ __forceinline__ T corr(T x, T f, const LineOp<T> &op, int n) {
 // tile geometry
 // ---------------------------------------------------------------------
 struct Tile {
-    long long base;   // global index of (line 0, position 0)
-    long long sl, sn; // strides between lines and along a line
+    unsigned base;    // global index of (line 0, position 0)
+    unsigned sl, sn;  // strides between lines and along a line
     int nlines;       // valid lines in this tile (<= L)
     int N;            // line length
     int ci, cj, ck;   // coordinates of (line 0, position 0)
@@ -253,24 +264,24 @@ struct Tile {
 template <int DIR>
 __device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
     Tile t;
-    const long long nxy = (long long)g.Nx * g.Ny;
+    const unsigned nxy = (unsigned)g.Nx * (unsigned)g.Ny;
     if (DIR == 0) {  // x-lines at rows j0.., plane k
         int j0 = blockIdx.x * L, k = blockIdx.y;
-        t.base = (long long)k * nxy + (long long)j0 * g.Nx;
+        t.base = (unsigned)k * nxy + (unsigned)j0 * g.Nx;
         t.sl = g.Nx; t.sn = 1;
         t.nlines = min(L, g.Ny - j0);
         t.N = g.Nx;
         t.ci = 0; t.cj = j0; t.ck = k;
     } else if (DIR == 1) {  // y-lines at columns i0.., plane k
         int i0 = blockIdx.x * L, k = blockIdx.y;
-        t.base = (long long)k * nxy + i0;
+        t.base = (unsigned)k * nxy + i0;
         t.sl = 1; t.sn = g.Nx;
         t.nlines = min(L, g.Nx - i0);
         t.N = g.Ny;
         t.ci = i0; t.cj = 0; t.ck = k;
     } else {  // z-lines at columns i0.., row j
         int i0 = blockIdx.x * L, j = blockIdx.y;
-        t.base = (long long)j * g.Nx + i0;
+        t.base = (unsigned)j * g.Nx + i0;
         t.sl = 1; t.sn = nxy;
         t.nlines = min(L, g.Nx - i0);
         t.N = g.Nz;
@@ -280,21 +291,28 @@ __device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
 }
 
 // Point p of a tile: consecutive threads touch consecutive global addresses
-// (position-major for x-lines, line-major otherwise).
+// (position-major for x-lines, line-major otherwise).  L is a power of two
+// (lgL its logarithm); division by the x-line length uses a precomputed
+// multiplier (divN: p / N = (umulhi(p, mul) + p) >> sh for p < 2^31).
 struct Pt {
-    long long gi;  // global index (a valid address even when !ok)
+    unsigned gi;   // global index (a valid address even when !ok)
     int o;         // shared-memory offset
     int l, n;
     bool ok;
 };
 
 template <int DIR>
-__device__ __forceinline__ Pt point(const Tile &t, int p, int L, int P) {
+__device__ __forceinline__ Pt point(const Tile &t, int p, int L, int P, int lgL, FastDiv dv) {
     Pt q;
-    if (DIR == 0) { q.l = p / t.N; q.n = p - q.l * t.N; }
-    else { q.n = p / L; q.l = p - q.n * L; }
+    if (DIR == 0) {
+        q.l = (int)((__umulhi((unsigned)p, dv.mul) + (unsigned)p) >> dv.sh);
+        q.n = p - q.l * t.N;
+    } else {
+        q.n = p >> lgL;
+        q.l = p & (L - 1);
+    }
     q.ok = q.l < t.nlines && q.n < t.N;
-    q.gi = q.ok ? t.base + q.l * t.sl + q.n * t.sn : t.base;
+    q.gi = q.ok ? t.base + (unsigned)q.l * t.sl + (unsigned)q.n * t.sn : t.base;
     q.o = q.n * P + q.l;
     return q;
 }
@@ -335,11 +353,51 @@ __device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem<T> s;
     s.P = P;
-    s.bstride = buf_stride(N, P, L, (int)(sizeof(T) / 4));
+    s.bstride = buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4));
     s.fact = reinterpret_cast<T *>(smem_raw);
     const int nf = (nbuf * L + 3) & ~3;
     s.buf = reinterpret_cast<T *>(smem_raw) + nf;
     return s;
+}
+
+// Per-thread loop over the points of a tile with a software pipeline: the
+// global loads of the thread's next point are issued before the current
+// point is computed, so memory latency overlaps the arithmetic.
+// ld(S&, p) loads point p; cp(S&) computes and stores it.
+template <typename S, typename LD, typename CP>
+__device__ __forceinline__ void pipelined(int NL, LD &&ld, CP &&cp) {
+    int p = threadIdx.x;
+    if (p >= NL) return;
+    S s0, s1;
+    ld(s0, p);
+    for (;;) {
+        const int p1 = p + blockDim.x;
+        if (p1 < NL) ld(s1, p1);
+        cp(s0);
+        if (p1 >= NL) break;
+        const int p2 = p1 + blockDim.x;
+        if (p2 < NL) ld(s0, p2);
+        cp(s1);
+        if (p2 >= NL) break;
+        p = p2;
+    }
+}
+
+// Per-thread loop over the points of a tile in batches of B: the loads of B
+// points are issued together, then the B points are computed and stored.
+template <typename S, int B, typename LD, typename CP>
+__device__ __forceinline__ void batched(int NL, LD &&ld, CP &&cp) {
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        S s[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int p = p0 + b * blockDim.x;
+            ld(s[b], p < NL ? p : p0);
+            if (p >= NL) s[b].pt.ok = false;
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) cp(s[b]);
+    }
 }
 
 // A task: solve A (src a, dst da, operator oa) and solve B, run together.
@@ -412,33 +470,24 @@ __device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_x(SweepArgs<T> a) {
-    constexpr int B = sizeof(T) == 4 ? 4 : 2;
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_x(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(XNB, L, P, N);
     const GasParams gp = a.gas;
-    const T *__restrict__ q0 = a.qs[0];
-    const T *__restrict__ q1 = a.qs[1];
-    const T *__restrict__ q2 = a.qs[2];
-    const T *__restrict__ q3 = a.qs[3];
-    const T *__restrict__ q4 = a.qs[4];
-    // phase A
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
-        Pt pt[B];
-        T v[B][5];
+    // phase A: primitives and the inputs of the x-solves
+    struct InA { Pt pt; T q[5]; };
+    batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
+        [&](InA &in, int p) {
+            in.pt = point<0>(t, p, L, P, a.lgL, a.divN);
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            pt[b] = point<0>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
-            v[b][0] = q0[gi]; v[b][1] = q1[gi]; v[b][2] = q2[gi]; v[b][3] = q3[gi]; v[b][4] = q4[gi];
-        }
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            if (!pt[b].ok) continue;
-            const long long gi = pt[b].gi;
-            PrimW<T> s = prim_w<T>(gp, v[b][0], v[b][1], v[b][2], v[b][3], v[b][4]);
+            for (int f = 0; f < 5; ++f) in.q[f] = a.qs[f][in.pt.gi];
+        },
+        [&](InA &in) {
+            if (!in.pt.ok) return;
+            const unsigned gi = in.pt.gi;
+            PrimW<T> s = prim_w<T>(gp, in.q[0], in.q[1], in.q[2], in.q[3], in.q[4]);
             a.prim[0][gi] = s.U; a.prim[1][gi] = s.V; a.prim[2][gi] = s.W;
             a.prim[3][gi] = s.p; a.prim[4][gi] = s.Tt;
             // stage-start primitives: on stage 1, points of SPONGE faces (not
@@ -447,14 +496,14 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_x(SweepAr
             PrimW<T> ss = s;
             if (a.use_backup) {
                 int i, j, k;
-                coords<0>(t, pt[b].l, pt[b].n, i, j, k);
+                coords<0>(t, in.pt.l, in.pt.n, i, j, k);
                 const int f = faces_of(a.g, i, j, k);
                 if ((f & a.sponge_kind_faces) && !(f & a.wall_faces))
                     ss = prim_w<T>(gp, to_work<T>(a.backup.f[0][gi]), to_work<T>(a.backup.f[1][gi]),
                                    to_work<T>(a.backup.f[2][gi]), to_work<T>(a.backup.f[3][gi]),
                                    to_work<T>(a.backup.f[4][gi]));
             }
-            const int o = pt[b].o;
+            const int o = in.pt.o;
             sm.b(XU)[o] = ss.U;
             sm.b(XV)[o] = ss.V;
             sm.b(XW)[o] = ss.W;
@@ -464,29 +513,25 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_x(SweepAr
             sm.b(XF2)[o] = s.rv * ss.U;
             sm.b(XF3)[o] = s.rw * ss.U;
             sm.b(XF4)[o] = s.re * ss.U + ss.U * ss.p;
-        }
-    }
+        });
     __syncthreads();
     run_tasks<T, 2>(sm, kTasksX, 7, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     // phase C
     const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
-        Pt pt[B];
-        T v[B][4];
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            pt[b] = point<0>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
-            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi]; v[b][3] = a.prim[4][gi];
-        }
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            if (!pt[b].ok) continue;
-            const Pt &p = pt[b];
-            const long long gi = p.gi;
+    struct InC { Pt pt; T v[4]; };
+    batched<InC, sizeof(T) == 4 ? 4 : 2>(NL,
+        [&](InC &in, int p) {
+            in.pt = point<0>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
+            in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi]; in.v[3] = a.prim[4][gi];
+        },
+        [&](InC &in) {
+            if (!in.pt.ok) return;
+            const Pt &p = in.pt;
+            const unsigned gi = p.gi;
             const Zn<T> zz = zn(a.d1, a.d2, p.n);
-            const T U = v[b][0], V = v[b][1], W = v[b][2], Tt = v[b][3];
+            const T U = in.v[0], V = in.v[1], W = in.v[2], Tt = in.v[3];
             const T mu = muref * pow(Tt, (T)0.76);
             const T amu = (T)0.76 * mu / Tt;
             a.mu[gi] = mu;
@@ -504,8 +549,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_x(SweepAr
             a.R[2][gi] = mu * Vxx - f2;
             a.R[3][gi] = mu * Wxx - f3;
             a.R[4][gi] = cpPr * mu * Txx + mu * (U * (c43 * Uxx) + V * Vxx + W * Wxx) - f4;
-        }
-    }
+        });
 }
 
 // ---------------------------------------------------------------------
@@ -518,68 +562,60 @@ __constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}
                                 {YF4, YF4, 0, YF4, YF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_y(SweepArgs<T> a) {
-    constexpr int B = sizeof(T) == 4 ? 4 : 2;
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(YNB, L, P, N);
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
-        Pt pt[B];
-        T v[B][11];
+    struct InA { Pt pt; T v[11]; };
+    batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
+        [&](InA &in, int p) {
+            in.pt = point<1>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            pt[b] = point<1>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
+            for (int f = 0; f < 4; ++f) in.v[f] = a.qs[f + 1][gi];
 #pragma unroll
-            for (int f = 0; f < 4; ++f) v[b][f] = a.qs[f + 1][gi];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.prim[f][gi];
-            v[b][9] = a.dx[0][gi];
-            v[b][10] = a.dx[1][gi];
-        }
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            if (!pt[b].ok) continue;
-            const int o = pt[b].o;
-            const T ru = v[b][0], rv = v[b][1], rw = v[b][2], re = v[b][3];
-            const T U = v[b][4], V = v[b][5], W = v[b][6], pp = v[b][7], Tt = v[b][8];
-            sm.b(YU)[o] = U;
+            for (int f = 0; f < 5; ++f) in.v[4 + f] = a.prim[f][gi];
+            in.v[9] = a.dx[0][gi];
+            in.v[10] = a.dx[1][gi];
+        },
+        [&](InA &in) {
+            if (!in.pt.ok) return;
+            const int o = in.pt.o;
+            const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
+            const T V = in.v[5], pp = in.v[7];
+            sm.b(YU)[o] = in.v[4];
             sm.b(YV)[o] = V;
-            sm.b(YW)[o] = W;
-            sm.b(YT)[o] = Tt;
-            sm.b(YUX)[o] = v[b][9];
-            sm.b(YVX)[o] = v[b][10];
+            sm.b(YW)[o] = in.v[6];
+            sm.b(YT)[o] = in.v[8];
+            sm.b(YUX)[o] = in.v[9];
+            sm.b(YVX)[o] = in.v[10];
             sm.b(YRV)[o] = rv;
             sm.b(YF1)[o] = ru * V;
             sm.b(YF2)[o] = rv * V + pp;
             sm.b(YF3)[o] = rw * V;
             sm.b(YF4)[o] = re * V + V * pp;
-        }
-    }
+        });
     __syncthreads();
     run_tasks<T, 2>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
-        Pt pt[B];
-        T v[B][9];
+    struct InC { Pt pt; T v[9]; };
+    batched<InC, 2>(NL,
+        [&](InC &in, int p) {
+            in.pt = point<1>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
+            in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi];
+            in.v[3] = a.mu[gi];
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
-            pt[b] = point<1>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
-            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi];
-            v[b][3] = a.mu[gi];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.R[f][gi];
-        }
-#pragma unroll
-        for (int b = 0; b < B; ++b) {
-            if (!pt[b].ok) continue;
-            const Pt &p = pt[b];
-            const long long gi = p.gi;
+            for (int f = 0; f < 5; ++f) in.v[4 + f] = a.R[f][gi];
+        },
+        [&](InC &in) {
+            if (!in.pt.ok) return;
+            const Pt &p = in.pt;
+            const unsigned gi = p.gi;
             const Zn<T> zz = zn(a.d1, a.d2, p.n);
-            const T U = v[b][0], V = v[b][1], W = v[b][2], mu = v[b][3];
+            const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3];
             const T Uy = gz(sm, YU, p, L, zz.z1), Uyy = gz(sm, YU2, p, L, zz.z2);
             const T Vy = gz(sm, YV, p, L, zz.z1), Vyy = gz(sm, YV2, p, L, zz.z2);
             const T Wy = gz(sm, YW, p, L, zz.z1), Wyy = gz(sm, YW2, p, L, zz.z2);
@@ -593,14 +629,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_y(SweepAr
             coords<1>(t, p.l, p.n, i, j, k);
             const int wd = a.wall_faces ? wall_dir(faces_of(a.g, i, j, k) & a.wall_faces) : -1;
             if (wd == 1) a.R[0][gi] = -cey;
-            else if (wd < 0) a.R[0][gi] = v[b][4] - cey;
-            a.R[1][gi] = v[b][5] + (mu * (Uyy + c13 * Vxy) - f1);
-            a.R[2][gi] = v[b][6] + (mu * (c43 * Vyy + c13 * Uxy) - f2);
-            a.R[3][gi] = v[b][7] + (mu * Wyy - f3);
-            a.R[4][gi] = v[b][8] +
+            else if (wd < 0) a.R[0][gi] = in.v[4] - cey;
+            a.R[1][gi] = in.v[5] + (mu * (Uyy + c13 * Vxy) - f1);
+            a.R[2][gi] = in.v[6] + (mu * (c43 * Vyy + c13 * Uxy) - f2);
+            a.R[3][gi] = in.v[7] + (mu * Wyy - f3);
+            a.R[4][gi] = in.v[8] +
                          (cpPr * mu * Tyy + mu * (U * Uyy + V * (c43 * Vyy) + W * Wyy + c13 * (U * Vxy + V * Uxy)) - f4);
-        }
-    }
+        });
 }
 
 // ---------------------------------------------------------------------
@@ -613,49 +648,43 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepArgs<T> a) {
-    constexpr int BA = sizeof(T) == 4 ? 4 : 2;
-    constexpr int BC = 2;
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_z(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<2>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(ZNB, L, P, N);
-    for (int p0 = threadIdx.x; p0 < NL; p0 += BA * blockDim.x) {
-        Pt pt[BA];
-        T v[BA][13];
+    struct InA { Pt pt; T v[13]; };
+    batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
+        [&](InA &in, int p) {
+            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
 #pragma unroll
-        for (int b = 0; b < BA; ++b) {
-            pt[b] = point<2>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
+            for (int f = 0; f < 4; ++f) in.v[f] = a.qs[f + 1][gi];
 #pragma unroll
-            for (int f = 0; f < 4; ++f) v[b][f] = a.qs[f + 1][gi];
-#pragma unroll
-            for (int f = 0; f < 5; ++f) v[b][4 + f] = a.prim[f][gi];
-            v[b][9] = a.dx[0][gi];
-            v[b][10] = a.dy[1][gi];
-            v[b][11] = a.dx[2][gi];
-            v[b][12] = a.dy[2][gi];
-        }
-#pragma unroll
-        for (int b = 0; b < BA; ++b) {
-            if (!pt[b].ok) continue;
-            const int o = pt[b].o;
-            const T ru = v[b][0], rv = v[b][1], rw = v[b][2], re = v[b][3];
-            const T U = v[b][4], V = v[b][5], W = v[b][6], pp = v[b][7], Tt = v[b][8];
-            sm.b(ZU)[o] = U;
-            sm.b(ZV)[o] = V;
+            for (int f = 0; f < 5; ++f) in.v[4 + f] = a.prim[f][gi];
+            in.v[9] = a.dx[0][gi];
+            in.v[10] = a.dy[1][gi];
+            in.v[11] = a.dx[2][gi];
+            in.v[12] = a.dy[2][gi];
+        },
+        [&](InA &in) {
+            if (!in.pt.ok) return;
+            const int o = in.pt.o;
+            const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
+            const T W = in.v[6], pp = in.v[7];
+            sm.b(ZU)[o] = in.v[4];
+            sm.b(ZV)[o] = in.v[5];
             sm.b(ZW)[o] = W;
-            sm.b(ZT)[o] = Tt;
-            sm.b(ZS)[o] = v[b][9] + v[b][10];
-            sm.b(ZWX)[o] = v[b][11];
-            sm.b(ZWY)[o] = v[b][12];
+            sm.b(ZT)[o] = in.v[8];
+            sm.b(ZS)[o] = in.v[9] + in.v[10];
+            sm.b(ZWX)[o] = in.v[11];
+            sm.b(ZWY)[o] = in.v[12];
             sm.b(ZRW)[o] = rw;
             sm.b(ZF1)[o] = ru * W;
             sm.b(ZF2)[o] = rv * W;
             sm.b(ZF3)[o] = rw * W + pp;
             sm.b(ZF4)[o] = re * W + W * pp;
-        }
-    }
+        });
     __syncthreads();
     run_tasks<T, 2>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
@@ -672,41 +701,38 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
     const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
     const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
     const bool need_qs = a.sponge || (a.mixed_rk4 && st == 1);
-    for (int p0 = threadIdx.x; p0 < NL; p0 += BC * blockDim.x) {
-        Pt pt[BC];
-        T v[BC][18];
-        double qa[BC][5], qb[BC][5], sav[BC][5], sgv[BC];
-        T qsv[BC][5];
-        float q1f[BC][5];
-        // all global loads of the batch first: no store can alias them
+    struct InC {
+        Pt pt;
+        T v[18];
+        double qa[5], qb[5];
+        T qsv[5];
+        float q1f[5];
+    };
+    pipelined<InC>(NL,
+        [&](InC &in, int p) {
+            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
+            in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi];
+            in.v[3] = a.mu[gi]; in.v[4] = a.amu[gi];
 #pragma unroll
-        for (int b = 0; b < BC; ++b) {
-            pt[b] = point<2>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
-            v[b][0] = a.prim[0][gi]; v[b][1] = a.prim[1][gi]; v[b][2] = a.prim[2][gi];
-            v[b][3] = a.mu[gi]; v[b][4] = a.amu[gi];
-#pragma unroll
-            for (int f = 0; f < 4; ++f) { v[b][5 + f] = a.dx[f][gi]; v[b][9 + f] = a.dy[f][gi]; }
+            for (int f = 0; f < 4; ++f) { in.v[5 + f] = a.dx[f][gi]; in.v[9 + f] = a.dy[f][gi]; }
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
-                v[b][13 + f] = a.R[f][gi];
-                qa[b][f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
-                qb[b][f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
-                q1f[b][f] = need_q1s ? a.q1s[f][gi] : 0.f;
-                qsv[b][f] = need_qs ? a.qs[f][gi] : T(0);
-                sav[b][f] = a.sponge ? a.savg.f[f][gi] : 0.0;
+                in.v[13 + f] = a.R[f][gi];
+                in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
+                in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
+                in.q1f[f] = need_q1s ? a.q1s[f][gi] : 0.f;
+                in.qsv[f] = need_qs ? a.qs[f][gi] : T(0);
             }
-            sgv[b] = a.sponge ? a.sigma[gi] : 0.0;
-        }
-#pragma unroll
-        for (int b = 0; b < BC; ++b) {
-            if (!pt[b].ok) continue;
-            const Pt &p = pt[b];
-            const long long gi = p.gi;
+        },
+        [&](InC &in) {
+            if (!in.pt.ok) return;
+            const Pt &p = in.pt;
+            const unsigned gi = p.gi;
             const Zn<T> zz = zn(a.d1, a.d2, p.n);
-            const T U = v[b][0], V = v[b][1], W = v[b][2], mu = v[b][3], amu = v[b][4];
-            const T Ux = v[b][5], Vx = v[b][6], Wx = v[b][7], Tx = v[b][8];
-            const T Uy = v[b][9], Vy = v[b][10], Wy = v[b][11], Ty = v[b][12];
+            const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3], amu = in.v[4];
+            const T Ux = in.v[5], Vx = in.v[6], Wx = in.v[7], Tx = in.v[8];
+            const T Uy = in.v[9], Vy = in.v[10], Wy = in.v[11], Ty = in.v[12];
             const T Uz = gz(sm, ZU, p, L, zz.z1), Uzz = gz(sm, ZU2, p, L, zz.z2);
             const T Vz = gz(sm, ZV, p, L, zz.z1), Vzz = gz(sm, ZV2, p, L, zz.z2);
             const T Wz = gz(sm, ZW, p, L, zz.z1), Wzz = gz(sm, ZW2, p, L, zz.z2);
@@ -717,19 +743,19 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
             const T f1 = gz(sm, ZF1, p, L, zz.z1), f2 = gz(sm, ZF2, p, L, zz.z1);
             const T f3 = gz(sm, ZF3, p, L, zz.z1), f4 = gz(sm, ZF4, p, L, zz.z1);
             T src[5] = {T(0), T(0), T(0), T(0), T(0)};
-            if (a.sponge) {
-                const T sg = to_work<T>(sgv[b]);
+            if (a.sponge) {  // sigma (avg - q), SpongeBC / CSolver_AWS.hpp:228
+                const T sg = to_work<T>(a.sigma[gi]);
 #pragma unroll
-                for (int f = 0; f < 5; ++f) src[f] = sg * (to_work<T>(sav[b][f]) - qsv[b][f]);
+                for (int f = 0; f < 5; ++f) src[f] = sg * (to_work<T>(a.savg.f[f][gi]) - in.qsv[f]);
             }
             const T MuX = amu * Tx, MuY = amu * Ty, MuZ = amu * Tz;
             T R[5];
-            R[0] = v[b][13];
-            R[1] = v[b][14] + mu * (Uzz + c13 * Wxz) - f1 + c43 * MuX * (Ux - T(0.5) * Vy - T(0.5) * Wz) +
+            R[0] = in.v[13];
+            R[1] = in.v[14] + mu * (Uzz + c13 * Wxz) - f1 + c43 * MuX * (Ux - T(0.5) * Vy - T(0.5) * Wz) +
                    MuY * (Uy + Vx) + MuZ * (Wx + Uz) + src[1];
-            R[2] = v[b][15] + mu * (Vzz + c13 * Wyz) - f2 + c43 * MuY * (Vy - T(0.5) * Ux - T(0.5) * Wz) +
+            R[2] = in.v[15] + mu * (Vzz + c13 * Wyz) - f2 + c43 * MuY * (Vy - T(0.5) * Ux - T(0.5) * Wz) +
                    MuX * (Uy + Vx) + MuZ * (Wy + Vz) + src[2];
-            R[3] = v[b][16] + mu * (c43 * Wzz + c13 * S) - f3 + c43 * MuZ * (Wz - T(0.5) * Ux - T(0.5) * Vy) +
+            R[3] = in.v[16] + mu * (c43 * Wzz + c13 * S) - f3 + c43 * MuZ * (Wz - T(0.5) * Ux - T(0.5) * Vy) +
                    MuX * (Wx + Uz) + MuY * (Wy + Vz) + src[3];
             const T q2s = Ux * Ux + Vy * Vy + Wz * Wz;
             const T sq = Uy * Uy + Uz * Uz + Vx * Vx + Vz * Vz + Wx * Wx + Wy * Wy;
@@ -741,7 +767,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
                          c23 * V * MuY * (Ux + Wz) - c23 * W * MuZ * (Ux + Vy) + U * MuY * (Uy + Vx) +
                          U * MuZ * (Uz + Wx) + V * MuX * (Uy + Vx) + V * MuZ * (Vz + Wy) + W * MuX * (Uz + Wx) +
                          W * MuY * (Vz + Wy);
-            R[4] = v[b][17] + cpPr * (MuX * Tx + MuY * Ty + MuZ * Tz + mu * Tzz) + v1 + v2 - f4 + T(2.0) * src[4];
+            R[4] = in.v[17] + cpPr * (MuX * Tx + MuY * Ty + MuZ * Tz + mu * Tzz) + v1 + v2 - f4 + T(2.0) * src[4];
             // continuity and the post-step boundary fix-up (CSolver_AWS.cpp:1506-1679)
             int i, j, k;
             coords<2>(t, p.l, p.n, i, j, k);
@@ -751,7 +777,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
             else if (wd < 0) R[0] = R[0] - cez + src[0];
             const bool zero_all = (fc & a.sponge_kind_faces) != 0;
             const bool zero_mom = wd >= 0;
-            // results of the point: stores only from here on
             if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
                 a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
             }
@@ -763,15 +788,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
                     if (zero_all || (f > 0 && zero_mom)) d = 0.0;
                     if (a.dq_out[0]) a.dq_out[f][gi] = d;
                     if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
-                        if (st == 1) a.qk.f[f][gi] = qa[b][f] + d;
-                        else if (st == 2) a.qk.f[f][gi] = 0.75 * qa[b][f] + 0.25 * qb[b][f] + 0.25 * d;
-                        else a.q2.f[f][gi] = (1.0 / 3.0) * qa[b][f] + (2.0 / 3.0) * qb[b][f] + (2.0 / 3.0) * d;
+                        if (st == 1) a.qk.f[f][gi] = in.qa[f] + d;
+                        else if (st == 2) a.qk.f[f][gi] = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * d;
+                        else a.q2.f[f][gi] = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * d;
                     } else {    // RK4 (RK4.hpp:35-118); qa = q1 (stage 1) or q2
                         const double ca = (st == 1 || st == 4) ? (1.0 / 6.0) : (1.0 / 3.0);
                         const double cb = (st == 3) ? 1.0 : 0.5;
-                        a.q2.f[f][gi] = qa[b][f] + ca * d;
-                        if (st == 1) a.qk.f[f][gi] = qa[b][f] + cb * d;
-                        else if (st < 4) a.qk.f[f][gi] = qb[b][f] + cb * d;
+                        a.q2.f[f][gi] = in.qa[f] + ca * d;
+                        if (st == 1) a.qk.f[f][gi] = in.qa[f] + cb * d;
+                        else if (st < 4) a.qk.f[f][gi] = in.qb[f] + cb * d;
                     }
                 }
             } else {
@@ -785,18 +810,18 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
                     if (tvd) {
                         const double dd = to_f64(d);
                         double nv;
-                        if (st == 1) { nv = qa[b][f] + dd; a.qk.f[f][gi] = nv; }
-                        else if (st == 2) { nv = 0.75 * qa[b][f] + 0.25 * qb[b][f] + 0.25 * dd; a.qk.f[f][gi] = nv; }
-                        else { nv = (1.0 / 3.0) * qa[b][f] + (2.0 / 3.0) * qb[b][f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
+                        if (st == 1) { nv = in.qa[f] + dd; a.qk.f[f][gi] = nv; }
+                        else if (st == 2) { nv = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * dd; a.qk.f[f][gi] = nv; }
+                        else { nv = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
                         if (a.shadow_target != SHADOW_NONE) a.shadow_out[f][gi] = narrow(nv);
                     } else {
                         const T ca = (st == 1 || st == 4) ? T(1.0 / 6.0) : T(1.0 / 3.0);
                         const T cb = (st == 3) ? T(1.0) : T(0.5);
-                        const double q2n = qa[b][f] + to_f64(ca * d);
+                        const double q2n = in.qa[f] + to_f64(ca * d);
                         a.q2.f[f][gi] = q2n;
                         if (st < 4) {
                             // the next stage input qk = q1 + cb*dq, kept as an FP32 shadow
-                            const T q1s = st == 1 ? qsv[b][f] : (T)q1f[b][f];
+                            const T q1s = st == 1 ? in.qsv[f] : (T)in.q1f[f];
                             a.shadow_out[f][gi] = fma(cb, d, q1s);
                         } else if (a.shadow_target == SHADOW_Q2) {
                             a.shadow_out[f][gi] = narrow(q2n);
@@ -804,8 +829,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2) k_sweep_z(SweepAr
                     }
                 }
             }
-        }
-    }
+        });
 }
 
 // ---------------------------------------------------------------------
@@ -829,8 +853,8 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
         T v[B][5];
 #pragma unroll
         for (int b = 0; b < B; ++b) {
-            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P);
-            const long long gi = pt[b].gi;
+            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P, a.lgL, a.divN);
+            const unsigned gi = pt[b].gi;
 #pragma unroll
             for (int f = 0; f < 5; ++f)
                 v[b][f] = a.src64.f[f] ? to_work<T>(a.src64.f[f][gi] - a.ref[f]) : a.src32[f][gi];
@@ -850,14 +874,14 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
         double q[B][5];
 #pragma unroll
         for (int b = 0; b < B; ++b) {
-            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P);
+            pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P, a.lgL, a.divN);
 #pragma unroll
             for (int f = 0; f < 5; ++f) q[b][f] = a.delta_from.f[f] ? a.delta_from.f[f][pt[b].gi] : 0.0;
         }
 #pragma unroll
         for (int b = 0; b < B; ++b) {
             if (!pt[b].ok) continue;
-            const long long gi = pt[b].gi;
+            const unsigned gi = pt[b].gi;
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
                 const T v = get(sm, f, pt[b], L, a.op);
@@ -914,7 +938,7 @@ __global__ void __launch_bounds__(128) k_line_op(LineOpArgs a) {
 template <typename T>
 static size_t tile_smem(int nbuf, int L, int P, int N) {
     const int nf = (nbuf * L + 3) & ~3;
-    return sizeof(T) * ((size_t)nf + (size_t)nbuf * buf_stride(N, P, L, (int)(sizeof(T) / 4)));
+    return sizeof(T) * ((size_t)nf + (size_t)nbuf * buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4)));
 }
 
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
