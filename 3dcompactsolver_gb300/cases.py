@@ -80,6 +80,10 @@ def hit(N, seed=0, mach_t=0.3, k0=8.0, precision=_abi.FP64, CFL=0.5, alphaF=0.49
     amp = np.zeros_like(K)
     nz = K > 0
     amp[nz] = np.sqrt(Ek[nz] / (4.0 * math.pi * K2[nz]))
+    # no energy on the Nyquist planes: the real part of the inverse transform
+    # would otherwise break the projection there
+    nyq = (np.abs(KX) == N // 2) | (np.abs(KY) == N // 2) | (np.abs(KZ) == N // 2)
+    amp[nyq] = 0.0
     comps = []
     for _ in range(3):
         ph = rng.uniform(0.0, 2.0 * math.pi, K.shape)

@@ -16,8 +16,7 @@ CASE_NAMES = ["tgv12", "wall", "wall_moving_sponge", "wall_tvdrk3", "shear"]
 
 def _case(cases, name):
     import importlib
-    gm = importlib.import_module("golden.make_golden") if False else None  # noqa: F841
-    _abi = __import__("importlib").import_module("3dcompactsolver_gb300._abi")
+    _abi = importlib.import_module("3dcompactsolver_gb300._abi")
     table = {
         "tgv12": lambda: cases.tgv(12),
         "wall": lambda: cases.wall_box((12, 10, 9)),
