@@ -8,6 +8,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 
 #include "../../include/cs3d.h"
 #include "cs3d_dev.cuh"
@@ -1144,5 +1145,51 @@ extern "C" int cs3d_tgv_quantities(cs3d_handle *h, double out[7]) {
     out[4] = s[1];
     out[5] = s[5];
     out[6] = std::sqrt(s[4]);
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// allocation-free kinetic energy (no handle, no cudaMalloc, no host heap)
+// ---------------------------------------------------------------------
+namespace {
+constexpr int kKeMaxDevices = 64;
+std::mutex g_ke_mu;
+double *g_ke_ptr[kKeMaxDevices] = {};
+}  // namespace
+
+extern "C" int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *rhoU_dev,
+                                           const double *rhoV_dev, const double *rhoW_dev,
+                                           long long npts, void *stream, double *ke) {
+    if (!rho_dev || !rhoU_dev || !rhoV_dev || !rhoW_dev || !ke) return fail(CS3D_ERR_ARG, "null argument");
+    if (npts < 1 || npts > 2147483647LL)
+        return fail(CS3D_ERR_SHAPE, "npts = %lld: the allocation-free kinetic energy takes 1 .. 2^31-1 points",
+                    npts);
+    int dev = -1;
+    CS3D_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kKeMaxDevices)
+        return fail(CS3D_ERR_ARG, "device %d: the allocation-free kinetic energy serves devices 0..%d", dev,
+                    kKeMaxDevices - 1);
+    const double *ptrs[4] = {rho_dev, rhoU_dev, rhoV_dev, rhoW_dev};
+    for (int f = 0; f < 4; ++f) {
+        cudaPointerAttributes at{};
+        CS3D_CUDA(cudaPointerGetAttributes(&at, ptrs[f]));
+        if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != dev)
+            return fail(CS3D_ERR_ARG, "array %d is not device memory of the current device %d", f, dev);
+    }
+    double *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_ke_mu);
+        if (!g_ke_ptr[dev]) {
+            // first call on this device: look up the static scratch once
+            double *p = nullptr;
+            CS3D_CUDA(ke_scratch_address(&p));
+            g_ke_ptr[dev] = p;
+        }
+        scratch = g_ke_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    CS3D_CUDA(launch_ke_noalloc(rho_dev, rhoU_dev, rhoV_dev, rhoW_dev, npts, scratch, s));
+    CS3D_CUDA(cudaMemcpyAsync(ke, scratch + kKeBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CS3D_CUDA(cudaStreamSynchronize(s));
     return CS3D_OK;
 }

@@ -156,6 +156,12 @@ cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s);
 cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s);
+// allocation-free kinetic energy: kKeBlocks partials + the sum in a static
+// device array whose address ke_scratch_address returns
+constexpr int kKeBlocks = 1024;
+cudaError_t ke_scratch_address(double **ptr);
+cudaError_t launch_ke_noalloc(const double *rho, const double *ru, const double *rv, const double *rw,
+                              long long npts, double *scratch, cudaStream_t s);
 cudaError_t launch_wall_pre(const BCArgs &a, cudaStream_t s);
 cudaError_t launch_cfl(const CflArgs &a, cudaStream_t s);
 cudaError_t launch_nan_scan(const CflArgs &a, cudaStream_t s);

@@ -383,4 +383,58 @@ cudaError_t launch_shadow(const ShadowArgs &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------
+// Kinetic energy without any allocation: the KEsum column of the
+// Taylor-Green diagnostics (CSolver_AWS.cpp:2175-2236) from four device
+// arrays, with its partial sums in a fixed file-scope scratch array instead
+// of handle memory.  Same launch shape, per-thread order and reduction tree
+// as k_tgv, so the two agree.  Every call writes all kKeBlocks partials and
+// the result before reading them: nothing in the scratch needs to start at
+// zero, and two calls that overlap on one device race on it.
+// ---------------------------------------------------------------------
+static __device__ __align__(256) double g_ke_scratch[kKeBlocks + 1];
+
+__global__ void k_ke_partials(const double *__restrict__ rho, const double *__restrict__ ru,
+                              const double *__restrict__ rv, const double *__restrict__ rw,
+                              long long npts, double *part) {
+    double s = 0.0;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        double r = rho[gi];
+        double U = ru[gi] / r, V = rv[gi] / r, W = rw[gi] / r;
+        s += r * (U * U + V * V + W * W) / 2.0;
+    }
+    __shared__ double red[32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+        part[blockIdx.x] = v;
+    }
+}
+
+// one thread adds the partials in block order, as the host does for k_tgv
+__global__ void k_ke_final(double *part) {
+    double s = 0.0;
+    for (int b = 0; b < kKeBlocks; ++b) s += part[b];
+    part[kKeBlocks] = s;
+}
+
+cudaError_t ke_scratch_address(double **ptr) {
+    return cudaGetSymbolAddress((void **)ptr, g_ke_scratch);
+}
+
+cudaError_t launch_ke_noalloc(const double *rho, const double *ru, const double *rv, const double *rw,
+                              long long npts, double *scratch, cudaStream_t s) {
+    k_ke_partials<<<kKeBlocks, 256, 0, s>>>(rho, ru, rv, rw, npts, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_ke_final<<<1, 1, 0, s>>>(scratch);
+    return cudaGetLastError();
+}
+
 }  // namespace cs3d

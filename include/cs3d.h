@@ -200,6 +200,25 @@ int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
  * requires CS3D_OPT_STORE_DIAGNOSTICS to have been on during that stage. */
 int cs3d_tgv_quantities(cs3d_handle *h, double out[7]);
 
+/* ---- allocation-free kinetic energy -------------------------------------
+ * No counterpart in the reference.  The KEsum column of
+ * cs3d_tgv_quantities (sum over points of rho |u|^2 / 2, CSolver_AWS.cpp:
+ * 2175-2236) from four FP64 device arrays of npts points, without a handle.
+ * For callers that may not allocate device memory: code whose device memory
+ * is all owned by another allocator (a caching pool), or that must not pay
+ * the device-wide synchronisation of cudaMalloc/cudaFree, or that has no
+ * solver handle (cs3d_create allocates).  This call allocates nothing, on the
+ * device or the host: its 1025 doubles (8200 bytes) of partial sums live in a
+ * fixed static device array.  The arrays must be device memory of the
+ * current device; the kernels run on `stream` (a cudaStream_t, NULL for the
+ * default stream) and the call returns after the result is in *ke.
+ * The first call on each device looks up the static array's address; make it
+ * before any stream capture starts.  Nothing has to be zeroed beforehand.
+ * Two calls that overlap in time on one device share the array and race.
+ * npts must be 1 .. 2^31-1 (CS3D_ERR_SHAPE otherwise). */
+int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *rhoU_dev, const double *rhoV_dev,
+                                const double *rhoW_dev, long long npts, void *stream, double *ke);
+
 #ifdef __cplusplus
 }
 #endif
