@@ -31,6 +31,8 @@ LIB_PATH = os.environ.get("CS3D_LIB_PATH") or os.path.join(HERE, "libcs3d_gb300.
 OPT_STORE_INCREMENTS = 1
 OPT_STORE_DIAGNOSTICS = 2
 OPT_KERNEL_TIMING = 3
+ADJ_SEED = 0       # cs3d_adjoint_backward: dJ/dq of the final state given
+ADJ_KE_MEAN = 1    # J = mean over points of rho |u|^2 / 2 of the final state
 KERNEL_CLASSES = ("sweep_x", "sweep_y", "sweep_z", "filter", "boundary", "cfl", "sponge", "other")
 
 _lib = None
@@ -75,6 +77,10 @@ def lib():
         L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
                                         ctypes.c_int]
         L.cs3d_version.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
+        L.cs3d_adjoint_record.argtypes = [_H, ctypes.c_int, ctypes.c_int]
+        L.cs3d_adjoint_backward.argtypes = [_H, ctypes.c_int, _DP, _DP, _DP]
+        L.cs3d_rhs_eval.argtypes = [_H, _DP, _DP]
+        L.cs3d_rhs_vjp.argtypes = [_H, _DP, _DP, _DP]
         _lib = L
     return _lib
 
@@ -183,11 +189,53 @@ class Solver:
         check(lib().cs3d_tgv_quantities(self.h, _dptr(out)))
         return out
 
+    # -- discrete adjoint (periodic, RK4, fixed dt, FP64) -------------------
+    def _q5(self, q):
+        a = np.ascontiguousarray(q, dtype=np.float64).reshape(-1)
+        if a.size != 5 * self.cfg.npts:
+            raise ValueError(f"expected 5 fields of {self.cfg.npts} points, got {a.size} values")
+        return a
+
+    def rhs_eval(self, q):
+        """R(q), the stage right-hand side from its 48 stored pointwise inputs."""
+        qa = self._q5(q)
+        out = np.empty((5,) + self.shape)
+        check(lib().cs3d_rhs_eval(self.h, _dptr(qa), _dptr(out)))
+        return out
+
+    def rhs_vjp(self, q, lam):
+        """(dR/dq)^T lam at the state q (both (5, Nz, Ny, Nx))."""
+        qa, la = self._q5(q), self._q5(lam)
+        out = np.empty((5,) + self.shape)
+        check(lib().cs3d_rhs_vjp(self.h, _dptr(qa), _dptr(la), _dptr(out)))
+        return out
+
+    def adjoint_record(self, nsteps, checkpoint_every=0):
+        """Run nsteps from the current state, keeping checkpoints for the adjoint."""
+        check(lib().cs3d_adjoint_record(self.h, int(nsteps), int(checkpoint_every)))
+
+    def adjoint_backward(self, objective=ADJ_KE_MEAN, seed=None):
+        """(dJ/dq0 as (5, Nz, Ny, Nx), J) for the recorded steps."""
+        grad = np.empty((5,) + self.shape)
+        J = ctypes.c_double(0.0)
+        keep = self._q5(seed) if seed is not None else None
+        sp = _dptr(keep) if keep is not None else None
+        check(lib().cs3d_adjoint_backward(self.h, int(objective), sp, _dptr(grad), ctypes.byref(J)))
+        return grad, J.value
+
     def line_op(self, kind, direction, in_ptr, out_ptr):
         """kind 1/2/3 = deriv1/deriv2/filter on device arrays in the direction's
         contiguous layout."""
         fn = {1: lib().cs3d_deriv1, 2: lib().cs3d_deriv2, 3: lib().cs3d_filter}[kind]
         check(fn(self.h, int(direction), ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr)))
+
+
+def ic_velocity_gradient(grad_q0, rho0, U0, V0, W0):
+    """dJ/dU0, dJ/dV0, dJ/dW0 from dJ/dq0 through the initial state
+    q0 = (rho0, rho0 U0, rho0 V0, rho0 W0, p0/(gamma-1) + rho0 |u0|^2 / 2)
+    of setInitialConditions (CSolver_AWS.cpp:199-504) on periodic grids."""
+    g = np.asarray(grad_q0).reshape((5,) + np.shape(rho0))
+    return (rho0 * (g[1] + U0 * g[4]), rho0 * (g[2] + V0 * g[4]), rho0 * (g[3] + W0 * g[4]))
 
 
 # ---------------------------------------------------------------------------

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libcs3d_gb300.so")
 OBJDIR = os.path.join(HERE, "_build")
-SOURCES = ["cs3d_sweeps.cu", "cs3d_point.cu", "cs3d_abi.cu"]
+SOURCES = ["cs3d_sweeps.cu", "cs3d_point.cu", "cs3d_abi.cu", "cs3d_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wno-enum-compare",
          f"-I{INC}"]

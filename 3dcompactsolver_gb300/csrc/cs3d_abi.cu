@@ -9,10 +9,12 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <initializer_list>
 
 #include "../../include/cs3d.h"
 #include "cs3d_dev.cuh"
 #include "cs3d_kernels.cuh"
+#include "cs3d_rhs_adjoint.cuh"  // kIn* slots of the adjoint tape
 
 using namespace cs3d;
 
@@ -257,6 +259,9 @@ struct DeviceGuard {
 // ---------------------------------------------------------------------
 // the handle
 // ---------------------------------------------------------------------
+// FP64 five-field groups of the adjoint workspace
+enum AdjField { ADJ_Y2 = 0, ADJ_Y3, ADJ_Y4, ADJ_QB, ADJ_QB2, ADJ_LAM, ADJ_YS, ADJ_YT, ADJ_FIN, kAdjFields };
+
 struct cs3d_handle {
     cs3d_config cfg;
     int dev = 0;
@@ -307,6 +312,19 @@ struct cs3d_handle {
     double *prim_out = nullptr;  // 7 FP64 fields for cs3d_get_field of primitives
     double *red = nullptr;       // reduction scratch
     std::vector<void *> allocs;
+    // discrete adjoint: workspace (allocated on first use) and the record of
+    // the forward steps (checkpoints every adj_every steps)
+    std::vector<void *> adj_allocs, adj_rec_allocs;
+    int adj_ws = 0;
+    void *adj_tape[48] = {}, *adj_gbar[48] = {}, *adj_flux[15] = {};
+    double *adj_f[kAdjFields][5] = {};
+    double *adj_part = nullptr;
+    int adj_nsteps = 0, adj_every = 0;
+    std::vector<double *> adj_ckpt;  // 5*npts each: the state before step k*adj_every
+    std::vector<int> adj_ts, adj_fts;
+    double *adj_seg = nullptr;       // adj_every states of the segment being reversed
+    int adj_end_ts = 0, adj_end_fts = 0;
+    double adj_end_scal[2] = {0, 0};
 };
 
 static cudaEvent_t ev_get(cs3d_handle *h) {
@@ -589,6 +607,8 @@ extern "C" int cs3d_destroy(cs3d_handle *h) {
     if (h->dq[0]) for (int f = 0; f < 5; f++) cudaFree(h->dq[f]);
     if (h->diag[0]) for (int f = 0; f < 3; f++) cudaFree(h->diag[f]);
     if (h->prim_out) cudaFree(h->prim_out);
+    for (void *p : h->adj_allocs) cudaFree(p);
+    for (void *p : h->adj_rec_allocs) cudaFree(p);
     for (auto &pe : h->ev_pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1191,5 +1211,442 @@ extern "C" int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *
     CS3D_CUDA(launch_ke_noalloc(rho_dev, rhoU_dev, rhoV_dev, rhoW_dev, npts, scratch, s));
     CS3D_CUDA(cudaMemcpyAsync(ke, scratch + kKeBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     CS3D_CUDA(cudaStreamSynchronize(s));
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// discrete adjoint of the time step (periodic boundaries, RK4, fixed dt)
+// ---------------------------------------------------------------------
+static int adj_check(cs3d_handle *h) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    for (int d = 0; d < 3; d++)
+        if (h->cfg.bc_type[d] != CS3D_PERIODIC_SOLVE)
+            return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only (direction %d)", d);
+    if (h->sponge || h->wall_faces) return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only");
+    if (h->mixed) return fail(CS3D_ERR_STATE, "the adjoint runs on CS3D_FP64 handles");
+    return CS3D_OK;
+}
+
+static int adj_alloc(cs3d_handle *h, std::vector<void *> &list, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(CS3D_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    list.push_back(*p);
+    return CS3D_OK;
+}
+
+static int adj_workspace(cs3d_handle *h) {
+    if (h->adj_ws) return CS3D_OK;
+    const size_t n = (size_t)h->g.npts;
+    int rc;
+    for (int i = 0; i < 48; i++) {
+        if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_tape[i], n * h->tb))) return rc;
+        if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_gbar[i], n * h->tb))) return rc;
+    }
+    for (int i = 0; i < 15; i++)
+        if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_flux[i], n * h->tb))) return rc;
+    for (int g = 0; g < kAdjFields; g++)
+        for (int f = 0; f < 5; f++)
+            if ((rc = adj_alloc(h, h->adj_allocs, (void **)&h->adj_f[g][f], n * 8))) return rc;
+    if ((rc = adj_alloc(h, h->adj_allocs, (void **)&h->adj_part, kKeSeedBlocks * 8))) return rc;
+    h->adj_ws = 1;
+    return CS3D_OK;
+}
+
+// one launch of k_apply along d: tasks {src, src2, dst, dst2, scale, op, acc}
+template <typename T>
+static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializer_list<ApplyTask<T>> tasks) {
+    ApplyArgs<T> a{};
+    a.g = h->g;
+    const int N = d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz;
+    a.ntask = (int)tasks.size();
+    a.L = pick_L(sizeof(T), a.ntask, N, d == 0 ? 1 : 0);
+    a.lgL = ilog2(a.L);
+    a.P = a.L + (d == 0 ? 1 : 0);
+    a.threads = 128;
+    a.divN = make_fastdiv((unsigned)N);
+    const DevOp<T> *ops = sizeof(T) == 8 ? reinterpret_cast<const DevOp<T> *>(h->op64[d])
+                                         : reinterpret_cast<const DevOp<T> *>(h->op32[d]);
+    a.op0 = ops[kind0].op;
+    a.op1 = ops[kind1].op;
+    int k = 0;
+    for (const ApplyTask<T> &t : tasks) a.t[k++] = t;
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_apply<T>(d, ops[kind0].op.H, a, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
+// tape G(q): primitives and the 44 derivative values of the right-hand side
+template <typename T>
+static int adj_tape(cs3d_handle *h, const T *const qin[5]) {
+    T **G = reinterpret_cast<T **>(h->adj_tape);
+    T **F = reinterpret_cast<T **>(h->adj_flux);
+    TapePrepArgs<T> pa{};
+    pa.g = h->g;
+    pa.gas = h->gas;
+    for (int f = 0; f < 5; f++) pa.qin[f] = qin[f];
+    for (int i = 0; i < 4; i++) pa.prim[i] = G[i];
+    for (int i = 0; i < 15; i++) pa.flux[i] = F[i];
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_tape_prep<T>(pa, h->stream));
+    tend(h);
+    const T one = T(1);
+    int rc;
+    // first and second derivatives of U V W T along d into slots b1.., b2..
+    auto derivs = [&](int d, int b1, int b2) {
+        return adj_apply<T>(h, d, 0, 1,
+                            {{G[0], nullptr, G[b1 + 0], nullptr, one, 0, 0}, {G[0], nullptr, G[b2 + 0], nullptr, one, 1, 0},
+                             {G[1], nullptr, G[b1 + 1], nullptr, one, 0, 0}, {G[1], nullptr, G[b2 + 1], nullptr, one, 1, 0},
+                             {G[2], nullptr, G[b1 + 2], nullptr, one, 0, 0}, {G[2], nullptr, G[b2 + 2], nullptr, one, 1, 0},
+                             {G[3], nullptr, G[b1 + 3], nullptr, one, 0, 0}, {G[3], nullptr, G[b2 + 3], nullptr, one, 1, 0}});
+    };
+    if ((rc = derivs(0, kInUx, kInUxx))) return rc;
+    if ((rc = adj_apply<T>(h, 0, 0, 1,
+                           {{F[0], nullptr, G[kInCEx], nullptr, one, 0, 0}, {F[1], nullptr, G[kInF1x], nullptr, one, 0, 0},
+                            {F[2], nullptr, G[kInF2x], nullptr, one, 0, 0}, {F[3], nullptr, G[kInF3x], nullptr, one, 0, 0},
+                            {F[4], nullptr, G[kInF4x], nullptr, one, 0, 0}})))
+        return rc;
+    if ((rc = derivs(1, kInUy, kInUyy))) return rc;
+    if ((rc = adj_apply<T>(h, 1, 0, 1,
+                           {{G[kInUx], nullptr, G[kInUxy], nullptr, one, 0, 0}, {G[kInVx], nullptr, G[kInVxy], nullptr, one, 0, 0},
+                            {F[5], nullptr, G[kInCEy], nullptr, one, 0, 0}, {F[6], nullptr, G[kInG1y], nullptr, one, 0, 0},
+                            {F[7], nullptr, G[kInG2y], nullptr, one, 0, 0}, {F[8], nullptr, G[kInG3y], nullptr, one, 0, 0},
+                            {F[9], nullptr, G[kInG4y], nullptr, one, 0, 0}})))
+        return rc;
+    if ((rc = derivs(2, kInUz, kInUzz))) return rc;
+    if ((rc = adj_apply<T>(h, 2, 0, 1,
+                           {{G[kInUx], G[kInVy], G[kInS], nullptr, one, 0, 0}, {G[kInWx], nullptr, G[kInWxz], nullptr, one, 0, 0},
+                            {G[kInWy], nullptr, G[kInWyz], nullptr, one, 0, 0}, {F[10], nullptr, G[kInCEz], nullptr, one, 0, 0},
+                            {F[11], nullptr, G[kInH1z], nullptr, one, 0, 0}, {F[12], nullptr, G[kInH2z], nullptr, one, 0, 0},
+                            {F[13], nullptr, G[kInH3z], nullptr, one, 0, 0}, {F[14], nullptr, G[kInH4z], nullptr, one, 0, 0}})))
+        return rc;
+    return CS3D_OK;
+}
+
+// out = J(q)^T lam for the right-hand side R(q) of one stage
+template <typename T>
+static int adj_rhs_vjp(cs3d_handle *h, const T *const qin[5], double *const lam[5], double *const out[5]) {
+    int rc = adj_tape<T>(h, qin);
+    if (rc) return rc;
+    T **G = reinterpret_cast<T **>(h->adj_tape);
+    T **B = reinterpret_cast<T **>(h->adj_gbar);
+    VjpArgs<T> va{};
+    va.g = h->g;
+    va.gas = h->gas;
+    for (int i = 0; i < 48; i++) {
+        va.tape[i] = G[i];
+        va.gbar[i] = B[i];
+    }
+    for (int f = 0; f < 5; f++) va.lam[f] = lam[f];
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_vjp<T>(va, h->stream));
+    tend(h);
+    // transposed operators, z then y then x: D1^T = -D1, D2^T = D2
+    const T m1 = T(-1), p1 = T(1);
+    auto derivsT = [&](int d, int b1, int b2) {
+        return adj_apply<T>(h, d, 0, 1,
+                            {{B[b1 + 0], nullptr, B[kInU], nullptr, m1, 0, 1}, {B[b2 + 0], nullptr, B[kInU], nullptr, p1, 1, 1},
+                             {B[b1 + 1], nullptr, B[kInV], nullptr, m1, 0, 1}, {B[b2 + 1], nullptr, B[kInV], nullptr, p1, 1, 1},
+                             {B[b1 + 2], nullptr, B[kInW], nullptr, m1, 0, 1}, {B[b2 + 2], nullptr, B[kInW], nullptr, p1, 1, 1},
+                             {B[b1 + 3], nullptr, B[kInT], nullptr, m1, 0, 1}, {B[b2 + 3], nullptr, B[kInT], nullptr, p1, 1, 1}});
+    };
+    if ((rc = derivsT(2, kInUz, kInUzz))) return rc;
+    if ((rc = adj_apply<T>(h, 2, 0, 1,
+                           {{B[kInS], nullptr, B[kInUx], B[kInVy], m1, 0, 1}, {B[kInWxz], nullptr, B[kInWx], nullptr, m1, 0, 1},
+                            {B[kInWyz], nullptr, B[kInWy], nullptr, m1, 0, 1}, {B[kInCEz], nullptr, B[kInCEz], nullptr, m1, 0, 0},
+                            {B[kInH1z], nullptr, B[kInH1z], nullptr, m1, 0, 0}, {B[kInH2z], nullptr, B[kInH2z], nullptr, m1, 0, 0},
+                            {B[kInH3z], nullptr, B[kInH3z], nullptr, m1, 0, 0}, {B[kInH4z], nullptr, B[kInH4z], nullptr, m1, 0, 0}})))
+        return rc;
+    if ((rc = derivsT(1, kInUy, kInUyy))) return rc;
+    if ((rc = adj_apply<T>(h, 1, 0, 1,
+                           {{B[kInUxy], nullptr, B[kInUx], nullptr, m1, 0, 1}, {B[kInVxy], nullptr, B[kInVx], nullptr, m1, 0, 1},
+                            {B[kInCEy], nullptr, B[kInCEy], nullptr, m1, 0, 0}, {B[kInG1y], nullptr, B[kInG1y], nullptr, m1, 0, 0},
+                            {B[kInG2y], nullptr, B[kInG2y], nullptr, m1, 0, 0}, {B[kInG3y], nullptr, B[kInG3y], nullptr, m1, 0, 0},
+                            {B[kInG4y], nullptr, B[kInG4y], nullptr, m1, 0, 0}})))
+        return rc;
+    if ((rc = derivsT(0, kInUx, kInUxx))) return rc;
+    if ((rc = adj_apply<T>(h, 0, 0, 1,
+                           {{B[kInCEx], nullptr, B[kInCEx], nullptr, m1, 0, 0}, {B[kInF1x], nullptr, B[kInF1x], nullptr, m1, 0, 0},
+                            {B[kInF2x], nullptr, B[kInF2x], nullptr, m1, 0, 0}, {B[kInF3x], nullptr, B[kInF3x], nullptr, m1, 0, 0},
+                            {B[kInF4x], nullptr, B[kInF4x], nullptr, m1, 0, 0}})))
+        return rc;
+    ChainArgs<T> ca{};
+    ca.g = h->g;
+    ca.gas = h->gas;
+    for (int f = 0; f < 5; f++) {
+        ca.qin[f] = qin[f];
+        ca.out[f] = out[f];
+    }
+    for (int i = 0; i < 48; i++) ca.gbar[i] = B[i];
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_chain<T>(ca, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
+// out = a x + b y + c z on five-field groups (y, z may be null)
+static int adj_lin(cs3d_handle *h, double *const out[5], double a, double *const x[5], double b,
+                   double *const y[5], double c = 0.0, double *const z[5] = nullptr) {
+    Lin5Args la{};
+    la.n = h->g.npts;
+    la.a = a; la.b = b; la.c = c;
+    for (int f = 0; f < 5; f++) {
+        la.out[f] = out[f];
+        la.x[f] = x[f];
+        la.y[f] = y ? y[f] : nullptr;
+        la.z[f] = z ? z[f] : nullptr;
+    }
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_lin5(la, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
+static int copy5(cs3d_handle *h, double *const dst[5], double *const src[5]) {
+    const size_t bytes = (size_t)h->g.npts * 8;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(dst[f], src[f], bytes, cudaMemcpyDeviceToDevice, h->stream));
+    return CS3D_OK;
+}
+
+static void slab5(cs3d_handle *h, double *base, double *out[5]) {
+    for (int f = 0; f < 5; f++) out[f] = base + (size_t)f * (size_t)h->g.npts;
+}
+
+// the filter order of filterConservedData for filter step number fts
+static void filter_order(int fts, int order[3]) {
+    const int m3 = fts % 3;
+    if (m3 == 1) { order[0] = 0; order[1] = 1; order[2] = 2; }
+    else if (m3 == 2) { order[0] = 1; order[1] = 2; order[2] = 0; }
+    else { order[0] = 2; order[1] = 0; order[2] = 1; }
+}
+
+// Adjoint of one time step taken from the state q0 with counters (ts, fts):
+// adj_f[ADJ_QB] holds dJ/dq after the step on entry and dJ/dq0 on return.
+static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
+    int rc;
+    double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
+    double **QB = h->adj_f[ADJ_QB], **QB2 = h->adj_f[ADJ_QB2], **LAM = h->adj_f[ADJ_LAM];
+    double **YS = h->adj_f[ADJ_YS], **YT = h->adj_f[ADJ_YT];
+    // stage inputs y2, y3, y4 of the forward step
+    h->timeStep = ts;
+    h->filterTimeStep = fts;
+    if ((rc = copy5(h, h->q1.f, q0))) return rc;
+    if ((rc = cs3d_pre_step(h))) return rc;
+    for (int st = 1; st <= 3; st++) {
+        if ((rc = run_stage<double>(h, st, 0))) return rc;
+        if ((rc = copy5(h, Y[st - 1], h->qk.f))) return rc;
+    }
+    const bool filtered = h->timeStep % h->cfg.filter_step == 0;
+    const double dt = h->cfg.dt_fixed;
+    // the filter's transpose: F = F_o2 F_o1 F_o0, F^T = F_o0 F_o1 F_o2 (each symmetric)
+    if ((rc = copy5(h, QB2, QB))) return rc;
+    if (filtered) {
+        int order[3];
+        filter_order(fts + 1, order);
+        for (int pass = 2; pass >= 0; pass--) {
+            const int d = order[pass];
+            if ((rc = adj_apply<double>(h, d, 2, 2,
+                                        {{QB2[0], nullptr, QB2[0], nullptr, 1.0, 0, 0},
+                                         {QB2[1], nullptr, QB2[1], nullptr, 1.0, 0, 0},
+                                         {QB2[2], nullptr, QB2[2], nullptr, 1.0, 0, 0},
+                                         {QB2[3], nullptr, QB2[3], nullptr, 1.0, 0, 0},
+                                         {QB2[4], nullptr, QB2[4], nullptr, 1.0, 0, 0}})))
+                return rc;
+        }
+    }
+    // RK4 (RK4.hpp:35-118) in reverse: q+ = q + dt/6 (k1 + 2 k2 + 2 k3 + k4),
+    // y2 = q + dt/2 k1, y3 = q + dt/2 k2, y4 = q + dt k3, k_s = R(y_s)
+    const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};  // weight of k_s in q+
+    const double cb[4] = {dt / 2.0, dt / 2.0, dt, 0.0};             // weight of k_s in y_{s+1}
+    double *const *yin[4] = {q0, Y[0], Y[1], Y[2]};
+    for (int s = 3; s >= 0; s--) {
+        // lam_s = ca_s qbar+ + cb_s ybar_{s+1}
+        if (s == 3) rc = adj_lin(h, LAM, ca[s], QB2, 0.0, nullptr);
+        else rc = adj_lin(h, LAM, ca[s], QB2, cb[s], YT);
+        if (rc) return rc;
+        if ((rc = adj_rhs_vjp<double>(h, yin[s], LAM, YT))) return rc;
+        if (s == 3) rc = copy5(h, YS, YT);
+        else rc = adj_lin(h, YS, 1.0, YS, 1.0, YT);
+        if (rc) return rc;
+    }
+    return adj_lin(h, QB, 1.0, QB2, 1.0, YS);
+}
+
+extern "C" int cs3d_adjoint_record(cs3d_handle *h, int nsteps, int checkpoint_every) {
+    int rc = adj_check(h);
+    if (rc) return rc;
+    if (!(h->cfg.dt_fixed > 0.0)) return fail(CS3D_ERR_STATE, "the adjoint needs a fixed time step (cfg.dt_fixed > 0)");
+    if (h->cfg.rk != CS3D_RK4) return fail(CS3D_ERR_STATE, "the adjoint is built for RK4");
+    if (nsteps < 1) return fail(CS3D_ERR_ARG, "nsteps = %d", nsteps);
+    if (checkpoint_every < 0) return fail(CS3D_ERR_ARG, "checkpoint_every = %d", checkpoint_every);
+    DeviceGuard dg(h->dev);
+    int every = checkpoint_every;
+    if (every == 0) every = (int)std::ceil(std::sqrt((double)nsteps));
+    if (every > nsteps) every = nsteps;
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    for (void *p : h->adj_rec_allocs) cudaFree(p);
+    h->adj_rec_allocs.clear();
+    h->adj_ckpt.clear();
+    h->adj_ts.clear();
+    h->adj_fts.clear();
+    h->adj_nsteps = 0;
+    if ((rc = adj_workspace(h))) return rc;
+    const size_t n5 = (size_t)h->g.npts * 5;
+    const int nseg = (nsteps + every - 1) / every;
+    for (int k = 0; k < nseg; k++) {
+        void *p = nullptr;
+        if ((rc = adj_alloc(h, h->adj_rec_allocs, &p, n5 * 8))) return rc;
+        h->adj_ckpt.push_back((double *)p);
+    }
+    if ((rc = adj_alloc(h, h->adj_rec_allocs, (void **)&h->adj_seg, n5 * 8 * (size_t)every))) return rc;
+    for (int k = 0; k < nsteps; k++) {
+        if (k % every == 0) {
+            double *ck[5];
+            slab5(h, h->adj_ckpt[k / every], ck);
+            if ((rc = copy5(h, ck, h->q1.f))) return rc;
+            h->adj_ts.push_back(h->timeStep);
+            h->adj_fts.push_back(h->filterTimeStep);
+        }
+        if ((rc = cs3d_step(h))) return rc;
+    }
+    h->adj_end_ts = h->timeStep;
+    h->adj_end_fts = h->filterTimeStep;
+    CS3D_CUDA(cudaMemcpyAsync(h->adj_end_scal, h->scal, 2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    h->adj_nsteps = nsteps;
+    h->adj_every = every;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double *seed_host, double *grad_host,
+                                     double *J) {
+    int rc = adj_check(h);
+    if (rc) return rc;
+    if (!h->adj_nsteps) return fail(CS3D_ERR_STATE, "call cs3d_adjoint_record first");
+    if (!grad_host) return fail(CS3D_ERR_ARG, "null gradient");
+    if (objective != CS3D_ADJ_SEED && objective != CS3D_ADJ_KE_MEAN)
+        return fail(CS3D_ERR_ARG, "objective = %d", objective);
+    if (objective == CS3D_ADJ_SEED && !seed_host) return fail(CS3D_ERR_ARG, "null seed");
+    if (h->timeStep != h->adj_end_ts) return fail(CS3D_ERR_STATE, "the solver has stepped since the record");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    double **QB = h->adj_f[ADJ_QB], **FIN = h->adj_f[ADJ_FIN];
+    // dJ/dq at the final state
+    if (objective == CS3D_ADJ_KE_MEAN) {
+        KeSeedArgs ka{};
+        ka.g = h->g;
+        ka.q = h->q1;
+        for (int f = 0; f < 5; f++) ka.seed[f] = QB[f];
+        ka.part = h->adj_part;
+        tstart(h, CS3D_K_OTHER);
+        CS3D_CUDA(launch_ke_seed(ka, h->stream));
+        tend(h);
+        double part[kKeSeedBlocks];
+        CS3D_CUDA(cudaMemcpyAsync(part, h->adj_part, sizeof(part), cudaMemcpyDeviceToHost, h->stream));
+        CS3D_CUDA(cudaStreamSynchronize(h->stream));
+        double s = 0.0;
+        for (int b = 0; b < kKeSeedBlocks; b++) s += part[b];
+        if (J) *J = s / (double)h->g.npts;
+    } else {
+        for (int f = 0; f < 5; f++)
+            CS3D_CUDA(cudaMemcpyAsync(QB[f], seed_host + (size_t)f * n, n * 8, cudaMemcpyHostToDevice, h->stream));
+        if (J) *J = 0.0;
+    }
+    if ((rc = copy5(h, FIN, h->q1.f))) return rc;
+    // segments in reverse: replay the segment's states from its checkpoint,
+    // then take the steps back one by one
+    const int every = h->adj_every, nsteps = h->adj_nsteps;
+    const int nseg = (nsteps + every - 1) / every;
+    std::vector<int> tsv(every), ftsv(every);
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int s0 = sg * every, m = std::min(nsteps, s0 + every) - s0;
+        double *st[5];
+        slab5(h, h->adj_seg, st);
+        double *ck[5];
+        slab5(h, h->adj_ckpt[sg], ck);
+        if ((rc = copy5(h, st, ck))) return rc;
+        h->timeStep = h->adj_ts[sg];
+        h->filterTimeStep = h->adj_fts[sg];
+        for (int j = 0; j < m; j++) {
+            tsv[j] = h->timeStep;
+            ftsv[j] = h->filterTimeStep;
+            if (j + 1 < m) {
+                double *cur[5], *nxt[5];
+                slab5(h, h->adj_seg + (size_t)j * 5 * n, cur);
+                slab5(h, h->adj_seg + (size_t)(j + 1) * 5 * n, nxt);
+                if ((rc = copy5(h, h->q1.f, cur))) return rc;
+                if ((rc = cs3d_step(h))) return rc;
+                if ((rc = copy5(h, nxt, h->q1.f))) return rc;
+            }
+        }
+        for (int j = m - 1; j >= 0; j--) {
+            double *cur[5];
+            slab5(h, h->adj_seg + (size_t)j * 5 * n, cur);
+            if ((rc = adj_step(h, tsv[j], ftsv[j], cur))) return rc;
+        }
+    }
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(grad_host + (size_t)f * n, QB[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
+    // back to the recorded final state
+    if ((rc = copy5(h, h->q1.f, FIN))) return rc;
+    h->timeStep = h->adj_end_ts;
+    h->filterTimeStep = h->adj_end_fts;
+    CS3D_CUDA(cudaMemcpyAsync(h->scal, h->adj_end_scal, 2 * 8, cudaMemcpyHostToDevice, h->stream));
+    if ((rc = launch_cfl_reduce(h))) return rc;
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+// R(q) from the tape, and J(q)^T lam, for one state given on the host
+static int adj_upload_state(cs3d_handle *h, const double *q_host, double *const dst[5]) {
+    const size_t n = (size_t)h->g.npts;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(dst[f], q_host + (size_t)f * n, n * 8, cudaMemcpyHostToDevice, h->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_rhs_eval(cs3d_handle *h, const double *q_host, double *R_host) {
+    int rc = adj_check(h);
+    if (rc) return rc;
+    if (!q_host || !R_host) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    if ((rc = adj_workspace(h))) return rc;
+    double **Q = h->adj_f[ADJ_Y2], **R = h->adj_f[ADJ_YT];
+    if ((rc = adj_upload_state(h, q_host, Q))) return rc;
+    if ((rc = adj_tape<double>(h, Q))) return rc;
+    RhsEvalArgs<double> ra{};
+    ra.g = h->g;
+    ra.gas = h->gas;
+    for (int i = 0; i < 48; i++) ra.tape[i] = (const double *)h->adj_tape[i];
+    for (int f = 0; f < 5; f++) ra.R[f] = R[f];
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_rhs_eval<double>(ra, h->stream));
+    tend(h);
+    const size_t n = (size_t)h->g.npts;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(R_host + (size_t)f * n, R[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_rhs_vjp(cs3d_handle *h, const double *q_host, const double *lam_host, double *out_host) {
+    int rc = adj_check(h);
+    if (rc) return rc;
+    if (!q_host || !lam_host || !out_host) return fail(CS3D_ERR_ARG, "null argument");
+    DeviceGuard dg(h->dev);
+    if ((rc = adj_workspace(h))) return rc;
+    double **Q = h->adj_f[ADJ_Y2], **LAM = h->adj_f[ADJ_LAM], **OUT = h->adj_f[ADJ_YT];
+    if ((rc = adj_upload_state(h, q_host, Q))) return rc;
+    if ((rc = adj_upload_state(h, lam_host, LAM))) return rc;
+    if ((rc = adj_rhs_vjp<double>(h, Q, LAM, OUT))) return rc;
+    const size_t n = (size_t)h->g.npts;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(out_host + (size_t)f * n, OUT[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }

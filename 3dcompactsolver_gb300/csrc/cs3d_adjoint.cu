@@ -1,0 +1,303 @@
+// cs3d_adjoint.cu -- kernels of the discrete adjoint of one RK stage
+// (sm_103a), periodic boundaries.
+//
+// The stage's right-hand side is R(q) = P(G(q)): G holds, per point, the
+// primitives U, V, W, T and 44 derivative values (first and second
+// derivatives of U, V, W, T along x, y, z; d/dx of the five x-fluxes and so
+// on; the cross derivatives Uxy, Vxy, d/dz(Ux+Vy), Wxz, Wyz), and P is the
+// pointwise combination of the sweep kernels.  Its transposed Jacobian is
+//
+//   J^T lam = C^T [ D^T (dP/dG)^T lam ]
+//
+// with dP/dG from the generated rhs_vjp, D^T the transposed line operators,
+// and C^T the pointwise chain rule through the fluxes and primitives.  On a
+// periodic uniform grid every compact operator is A^-1 B with A and B
+// circulant; A is symmetric, B of the 1st derivative antisymmetric and B of
+// the 2nd derivative and the filter symmetric, and circulants commute, so
+//   D1^T = -D1,  D2^T = D2,  F^T = F,
+// which k_apply evaluates with the forward solve and a sign.
+#include <cstdio>
+#include <cmath>
+#include "cs3d_tile.cuh"
+#include "cs3d_rhs_adjoint.cuh"
+
+namespace cs3d {
+
+// ---------------------------------------------------------------------
+// line operators along DIR on XYZ-layout fields
+// ---------------------------------------------------------------------
+template <typename T, int DIR, int H>
+__global__ void __launch_bounds__(128) k_apply(ApplyArgs<T> a) {
+    const int L = a.L, P = a.P;
+    const Tile t = make_tile<DIR>(a.g, L);
+    const int N = t.N, NL = N * L;
+    const int nt = a.ntask;
+    Smem<T> sm = smem_layout<T>(nt, L, P, N);
+    __shared__ Task tasks[kApplyMax / 2];
+    if ((int)threadIdx.x < (nt + 1) / 2) {
+        const int i = 2 * threadIdx.x, j = min(i + 1, nt - 1);
+        tasks[threadIdx.x] = Task{(signed char)i, (signed char)i, (signed char)a.t[i].op,
+                                  (signed char)j, (signed char)j, (signed char)a.t[j].op};
+    }
+    for (int p = threadIdx.x; p < NL; p += blockDim.x) {
+        const Pt pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+        if (!pt.ok) continue;
+        for (int k = 0; k < nt; ++k) {
+            T v = a.t[k].src[pt.gi];
+            if (a.t[k].src2) v += a.t[k].src2[pt.gi];
+            sm.b(k)[pt.o] = v;
+        }
+    }
+    __syncthreads();
+    run_tasks<T, H>(sm, tasks, (nt + 1) / 2, L, t.nlines, a.op0, a.op1);
+    __syncthreads();
+    for (int p = threadIdx.x; p < NL; p += blockDim.x) {
+        const Pt pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+        if (!pt.ok) continue;
+        for (int k = 0; k < nt; ++k) {
+            const ApplyTask<T> &tk = a.t[k];
+            const T v = tk.scale * get(sm, k, pt, L, tk.op == 1 ? a.op1 : a.op0);
+            if (tk.dst) tk.dst[pt.gi] = tk.acc ? tk.dst[pt.gi] + v : v;
+            if (tk.dst2) tk.dst2[pt.gi] = tk.dst2[pt.gi] + v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// pointwise parts
+// ---------------------------------------------------------------------
+__device__ __forceinline__ long long gstride() { return (long long)gridDim.x * blockDim.x; }
+__device__ __forceinline__ long long gfirst() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+
+// primitives and the Euler fluxes of the sweeps (the x, y, z phase A inputs)
+template <typename T>
+__global__ void k_tape_prep(TapePrepArgs<T> a) {
+    for (long long gi = gfirst(); gi < a.g.npts; gi += gstride()) {
+        const PrimW<T> s = prim_w<T>(a.gas, a.qin[0][gi], a.qin[1][gi], a.qin[2][gi], a.qin[3][gi], a.qin[4][gi]);
+        a.prim[0][gi] = s.U; a.prim[1][gi] = s.V; a.prim[2][gi] = s.W; a.prim[3][gi] = s.Tt;
+        a.flux[0][gi] = s.ru;
+        a.flux[1][gi] = s.ru * s.U + s.p;
+        a.flux[2][gi] = s.rv * s.U;
+        a.flux[3][gi] = s.rw * s.U;
+        a.flux[4][gi] = s.re * s.U + s.U * s.p;
+        a.flux[5][gi] = s.rv;
+        a.flux[6][gi] = s.ru * s.V;
+        a.flux[7][gi] = s.rv * s.V + s.p;
+        a.flux[8][gi] = s.rw * s.V;
+        a.flux[9][gi] = s.re * s.V + s.V * s.p;
+        a.flux[10][gi] = s.rw;
+        a.flux[11][gi] = s.ru * s.W;
+        a.flux[12][gi] = s.rv * s.W;
+        a.flux[13][gi] = s.rw * s.W + s.p;
+        a.flux[14][gi] = s.re * s.W + s.W * s.p;
+    }
+}
+
+// gbar = (dP/dG)^T lam at every point
+template <typename T>
+__global__ void __launch_bounds__(128) k_vjp(VjpArgs<T> a) {
+    const T muref = (T)a.gas.mu_ref, cpPr = (T)a.gas.cpPr;
+    for (long long gi = gfirst(); gi < a.g.npts; gi += gstride()) {
+        T in[kRhsIn], l[5], out[kRhsIn];
+#pragma unroll
+        for (int i = 0; i < kRhsIn; ++i) in[i] = a.tape[i][gi];
+#pragma unroll
+        for (int f = 0; f < 5; ++f) l[f] = (T)a.lam[f][gi];
+        rhs_vjp<T>(in, l, muref, cpPr, out);
+#pragma unroll
+        for (int i = 0; i < kRhsIn; ++i) a.gbar[i][gi] = out[i];
+    }
+}
+
+// R = P(G): the right-hand side from the tape (checks the tape)
+template <typename T>
+__global__ void k_rhs_eval(RhsEvalArgs<T> a) {
+    const T muref = (T)a.gas.mu_ref, cpPr = (T)a.gas.cpPr;
+    for (long long gi = gfirst(); gi < a.g.npts; gi += gstride()) {
+        T in[kRhsIn], R[5];
+#pragma unroll
+        for (int i = 0; i < kRhsIn; ++i) in[i] = a.tape[i][gi];
+        rhs_eval<T>(in, muref, cpPr, R);
+#pragma unroll
+        for (int f = 0; f < 5; ++f) a.R[f][gi] = (double)R[f];
+    }
+}
+
+// out = C^T gbar: the flux cotangents (gbar slots of CEx..F4x, CEy..G4y,
+// CEz..H4z after the transposed operators) and the primitive cotangents
+// (slots U, V, W, T) taken back to the conserved variables through
+//   fluxes  x: rhoU, rhoU U + p, rhoV U, rhoW U, (rhoE + p) U  (y, z alike)
+//   U = rhoU/rho, ..., p = (gamma-1)(rhoE - (rhoU^2+rhoV^2+rhoW^2)/(2 rho)),
+//   T = p / (rho R).
+template <typename T>
+__global__ void k_chain(ChainArgs<T> a) {
+    const T gm1 = (T)a.gas.gm1, Rg = (T)a.gas.R;
+    for (long long gi = gfirst(); gi < a.g.npts; gi += gstride()) {
+        const PrimW<T> s = prim_w<T>(a.gas, a.qin[0][gi], a.qin[1][gi], a.qin[2][gi], a.qin[3][gi], a.qin[4][gi]);
+        const T r = a.qin[0][gi];
+        const T U = s.U, V = s.V, W = s.W, p = s.p;
+        const T ru = s.ru, rv = s.rv, rw = s.rw, rep = s.re + s.p;
+        T ax[5], ay[5], az[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            ax[k] = a.gbar[kInCEx + k][gi];
+            ay[k] = a.gbar[kInCEy + k][gi];
+            az[k] = a.gbar[kInCEz + k][gi];
+        }
+        T gU = a.gbar[kInU][gi], gV = a.gbar[kInV][gi], gW = a.gbar[kInW][gi];
+        const T gT = a.gbar[kInT][gi];
+        T gr = T(0), gru = T(0), grv = T(0), grw = T(0), gre = T(0), gp = T(0);
+        // x fluxes
+        gru += ax[0] + ax[1] * U;
+        grv += ax[2] * U;
+        grw += ax[3] * U;
+        gre += ax[4] * U;
+        gU += ax[1] * ru + ax[2] * rv + ax[3] * rw + ax[4] * rep;
+        gp += ax[1] + ax[4] * U;
+        // y fluxes
+        grv += ay[0] + ay[2] * V;
+        gru += ay[1] * V;
+        grw += ay[3] * V;
+        gre += ay[4] * V;
+        gV += ay[1] * ru + ay[2] * rv + ay[3] * rw + ay[4] * rep;
+        gp += ay[2] + ay[4] * V;
+        // z fluxes
+        grw += az[0] + az[3] * W;
+        gru += az[1] * W;
+        grv += az[2] * W;
+        gre += az[4] * W;
+        gW += az[1] * ru + az[2] * rv + az[3] * rw + az[4] * rep;
+        gp += az[3] + az[4] * W;
+        // T = p / (rho R)
+        gp += gT / (r * Rg);
+        gr -= gT * s.Tt / r;
+        // primitives -> conserved
+        const T ir = T(1) / r;
+        gr += -(U * gU + V * gV + W * gW) * ir + gp * gm1 * T(0.5) * (U * U + V * V + W * W);
+        gru += gU * ir - gm1 * U * gp;
+        grv += gV * ir - gm1 * V * gp;
+        grw += gW * ir - gm1 * W * gp;
+        gre += gm1 * gp;
+        a.out[0][gi] = (double)gr;
+        a.out[1][gi] = (double)gru;
+        a.out[2][gi] = (double)grv;
+        a.out[3][gi] = (double)grw;
+        a.out[4][gi] = (double)gre;
+    }
+}
+
+__global__ void k_lin5(Lin5Args a) {
+    for (long long i = gfirst(); i < a.n; i += gstride()) {
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            double v = a.a * a.x[f][i];
+            if (a.y[f]) v += a.b * a.y[f][i];
+            if (a.z[f]) v += a.c * a.z[f][i];
+            a.out[f][i] = v;
+        }
+    }
+}
+
+__global__ void k_ke_seed(KeSeedArgs a) {
+    const double inv_n = 1.0 / (double)a.g.npts;
+    double s = 0.0;
+    for (long long gi = gfirst(); gi < a.g.npts; gi += gstride()) {
+        const double r = a.q.f[0][gi];
+        const double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+        const double k2 = U * U + V * V + W * W;
+        s += r * k2 / 2.0;
+        a.seed[0][gi] = -0.5 * k2 * inv_n;
+        a.seed[1][gi] = U * inv_n;
+        a.seed[2][gi] = V * inv_n;
+        a.seed[3][gi] = W * inv_n;
+        a.seed[4][gi] = 0.0;
+    }
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+        a.part[blockIdx.x] = v;
+    }
+}
+
+// ---------------------------------------------------------------------
+// launches
+// ---------------------------------------------------------------------
+static int pw_grid(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 152 * 8) b = 152 * 8;
+    return (int)(b < 1 ? 1 : b);
+}
+
+template <typename K, typename A>
+static cudaError_t tile_launch(K kernel, const A &a, dim3 grid, size_t sm, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    kernel<<<grid, a.threads, sm, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s) {
+    if (a.ntask < 1 || a.ntask > kApplyMax) return cudaErrorInvalidValue;
+    const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
+    const size_t sm = sweep_smem_bytes((int)sizeof(T), a.ntask, a.L, a.P, N);
+    const int L = a.L;
+    dim3 grid = dir == 0 ? dim3((a.g.Ny + L - 1) / L, a.g.Nz)
+                         : dir == 1 ? dim3((a.g.Nx + L - 1) / L, a.g.Nz) : dim3((a.g.Nx + L - 1) / L, a.g.Ny);
+    if (H == 4) {
+        if (dir == 0) return tile_launch(k_apply<T, 0, 4>, a, grid, sm, s);
+        if (dir == 1) return tile_launch(k_apply<T, 1, 4>, a, grid, sm, s);
+        return tile_launch(k_apply<T, 2, 4>, a, grid, sm, s);
+    }
+    if (dir == 0) return tile_launch(k_apply<T, 0, 2>, a, grid, sm, s);
+    if (dir == 1) return tile_launch(k_apply<T, 1, 2>, a, grid, sm, s);
+    return tile_launch(k_apply<T, 2, 2>, a, grid, sm, s);
+}
+
+template <typename T>
+cudaError_t launch_tape_prep(const TapePrepArgs<T> &a, cudaStream_t s) {
+    k_tape_prep<T><<<pw_grid(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_vjp(const VjpArgs<T> &a, cudaStream_t s) {
+    k_vjp<T><<<pw_grid(a.g.npts, 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_chain(const ChainArgs<T> &a, cudaStream_t s) {
+    k_chain<T><<<pw_grid(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_rhs_eval(const RhsEvalArgs<T> &a, cudaStream_t s) {
+    k_rhs_eval<T><<<pw_grid(a.g.npts, 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_lin5(const Lin5Args &a, cudaStream_t s) {
+    k_lin5<<<pw_grid(a.n, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_ke_seed(const KeSeedArgs &a, cudaStream_t s) {
+    k_ke_seed<<<kKeSeedBlocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_apply<double>(int, int, const ApplyArgs<double> &, cudaStream_t);
+template cudaError_t launch_apply<float>(int, int, const ApplyArgs<float> &, cudaStream_t);
+template cudaError_t launch_tape_prep<double>(const TapePrepArgs<double> &, cudaStream_t);
+template cudaError_t launch_tape_prep<float>(const TapePrepArgs<float> &, cudaStream_t);
+template cudaError_t launch_vjp<double>(const VjpArgs<double> &, cudaStream_t);
+template cudaError_t launch_vjp<float>(const VjpArgs<float> &, cudaStream_t);
+template cudaError_t launch_chain<double>(const ChainArgs<double> &, cudaStream_t);
+template cudaError_t launch_chain<float>(const ChainArgs<float> &, cudaStream_t);
+template cudaError_t launch_rhs_eval<double>(const RhsEvalArgs<double> &, cudaStream_t);
+template cudaError_t launch_rhs_eval<float>(const RhsEvalArgs<float> &, cudaStream_t);
+
+}  // namespace cs3d

@@ -173,6 +173,91 @@ cudaError_t launch_ic_wall_eos(const IcArgs &a, cudaStream_t s);
 cudaError_t launch_primitives(const PrimArgs &a, cudaStream_t s);
 cudaError_t launch_shadow(const ShadowArgs &a, cudaStream_t s);
 
+// ---------------------------------------------------------------------
+// discrete adjoint of the stage (periodic boundaries)
+// ---------------------------------------------------------------------
+// k_apply: up to kApplyMax line operators along one direction on XYZ-layout
+// fields; task k reads src (+ src2), applies op0 or op1, scales, and writes
+// or adds the result to dst, and adds it to dst2.  Each tile reads and
+// writes only its own points, so src and dst may be the same array.
+constexpr int kApplyMax = 8;
+template <typename T>
+struct ApplyTask {
+    const T *src, *src2;
+    T *dst, *dst2;
+    T scale;
+    int op;   // 0: op0, 1: op1
+    int acc;  // 1: dst += v, 0: dst = v
+};
+template <typename T>
+struct ApplyArgs {
+    Geom g;
+    int L, lgL, P, threads;
+    FastDiv divN;
+    LineOp<T> op0, op1;
+    int ntask;
+    ApplyTask<T> t[kApplyMax];
+};
+// primitives U V W T and the 15 Euler fluxes of the state q, in the work type
+template <typename T>
+struct TapePrepArgs {
+    Geom g;
+    GasParams gas;
+    const T *qin[5];  // the state in the work type (FP64 q, or the FP32 shadow)
+    T *prim[4];
+    T *flux[15];  // x: rhoU, rhoU U + p, rhoV U, rhoW U, (rhoE + p) U; then y, z
+};
+template <typename T>
+struct VjpArgs {
+    Geom g;
+    GasParams gas;
+    const T *tape[48];
+    const double *lam[5];
+    T *gbar[48];
+};
+template <typename T>
+struct ChainArgs {
+    Geom g;
+    GasParams gas;
+    const T *qin[5];
+    const T *gbar[48];
+    double *out[5];
+};
+template <typename T>
+struct RhsEvalArgs {
+    Geom g;
+    GasParams gas;
+    const T *tape[48];
+    double *R[5];
+};
+// out = a x + b y (+ c z) on five fields; y, z may be null
+struct Lin5Args {
+    long long n;
+    double *out[5];
+    const double *x[5], *y[5], *z[5];
+    double a, b, c;
+};
+// seed of J = mean over points of rho |u|^2 / 2, and per-block partial sums of J
+struct KeSeedArgs {
+    Geom g;
+    Q5 q;
+    double *seed[5];
+    double *part;
+};
+template <typename T>
+cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_tape_prep(const TapePrepArgs<T> &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_vjp(const VjpArgs<T> &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_chain(const ChainArgs<T> &a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_rhs_eval(const RhsEvalArgs<T> &a, cudaStream_t s);
+cudaError_t launch_lin5(const Lin5Args &a, cudaStream_t s);
+constexpr int kKeSeedBlocks = 512;
+cudaError_t launch_ke_seed(const KeSeedArgs &a, cudaStream_t s);
+
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N);
 int sweep_nbuf(int dir);
 int sweep_ntask(int dir);

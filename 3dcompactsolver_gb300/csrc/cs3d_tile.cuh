@@ -1,0 +1,429 @@
+// cs3d_tile.cuh -- pencil-tile machinery shared by the stage sweeps and the
+// adjoint kernels: chunked Thomas line solves with the cyclic correction,
+// tile geometry, shared-memory layout, point loops and primitives.
+#pragma once
+#include "cs3d_dev.cuh"
+#include "cs3d_kernels.cuh"
+
+namespace cs3d {
+
+// ---------------------------------------------------------------------
+// line solves
+// ---------------------------------------------------------------------
+constexpr int kU = 4;  // rows per unrolled chunk
+// Rows of padding after each line buffer in shared memory, so that the
+// chunked forward pass may read ahead past the line's end without a test.
+constexpr int kPad = 2 * kU + kMaxH + 2;
+
+// The first H and last H rows of the right-hand side, from explicit rows.
+template <typename T, int H>
+__device__ __forceinline__ void boundary_rows(const T *src, int P, const LineOp<T> &op, T pre[2 * H]) {
+    const int N = op.N;
+#pragma unroll
+    for (int b = 0; b < 2 * H; ++b) {
+        const int col = op.boff[b];
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < kTaps; ++k) {
+            int cc = col + k;
+            cc = cc < 0 ? cc + N : (cc >= N ? cc - N : cc);
+            acc = fma(op.btaps[b][k], src[cc * P], acc);
+        }
+        pre[b] = acc;
+    }
+}
+
+// Two line solves, A and B, run interleaved by one thread.  Each reads its
+// line from s* (stride P) and writes the uncorrected solution to d*, which may
+// alias s*: the forward pass reads positions beyond the rows it writes, and
+// the boundary rows are formed before any write.  B may also read A's source
+// (1st and 2nd derivative of one field: A in place, B into its own buffer).
+// The Sherman-Morrison factor of a periodic line is formed in FP64 from the
+// line's end values and stored to f* in the work precision.
+template <typename T, int H>
+__device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &oa, T *fa, const T *sb, T *db,
+                                           const LineOp<T> &ob, T *fb, int P) {
+    constexpr int W = 2 * H + 1;
+    const int N = oa.N;
+    T pa[2 * H], pb[2 * H];
+    boundary_rows<T, H>(sa, P, oa, pa);
+    boundary_rows<T, H>(sb, P, ob, pb);
+    T ta[W], tb[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        ta[k] = oa.taps[kMaxH - H + k];
+        tb[k] = ob.taps[kMaxH - H + k];
+    }
+    const T *__restrict__ ma = oa.m;
+    const T *__restrict__ mb = ob.m;
+    // window of the first interior row H: positions 0..2H
+    T wa[W], wb[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        wa[k] = sa[k * P];
+        wb[k] = sb[k * P];
+    }
+    // rows 0..H-1
+    T ya = pa[0], yb = pb[0];
+    da[0] = ya;
+    db[0] = yb;
+#pragma unroll
+    for (int n = 1; n < H; ++n) {
+        ya = fma(-__ldg(&ma[n]), ya, pa[n]);
+        yb = fma(-__ldg(&mb[n]), yb, pb[n]);
+        da[n * P] = ya;
+        db[n * P] = yb;
+    }
+    // interior rows H..N-H-1 in chunks of kU, next chunk prefetched
+    const int nend = N - H;
+    int n = H;
+    T na[kU], nb[kU], mna[kU], mnb[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+        const int pos = n + H + 1 + j;
+        na[j] = sa[pos * P];
+        nb[j] = sb[pos * P];
+    }
+    load4(oa.mf, mna);
+    load4(ob.mf, mnb);
+#pragma unroll 2
+    for (; n + kU <= nend; n += kU) {
+        T ca[kU], cb[kU], mca[kU], mcb[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            ca[j] = na[j]; cb[j] = nb[j]; mca[j] = mna[j]; mcb[j] = mnb[j];
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const int pos = n + kU + H + 1 + j;
+            na[j] = sa[pos * P];
+            nb[j] = sb[pos * P];
+        }
+        load4(oa.mf + (n + kU - H), mna);
+        load4(ob.mf + (n + kU - H), mnb);
+        T ea[W + kU], eb[W + kU];
+#pragma unroll
+        for (int k = 0; k < W; ++k) { ea[k] = wa[k]; eb[k] = wb[k]; }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) { ea[W + j] = ca[j]; eb[W + j] = cb[j]; }
+        T ra[kU], rb[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            T acc_a = T(0), acc_b = T(0);
+#pragma unroll
+            for (int k = 0; k < W; ++k) {
+                acc_a = fma(ta[k], ea[j + k], acc_a);
+                acc_b = fma(tb[k], eb[j + k], acc_b);
+            }
+            ra[j] = acc_a;
+            rb[j] = acc_b;
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            ya = fma(-mca[j], ya, ra[j]);
+            yb = fma(-mcb[j], yb, rb[j]);
+            da[(n + j) * P] = ya;
+            db[(n + j) * P] = yb;
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) { wa[k] = ea[kU + k]; wb[k] = eb[kU + k]; }
+    }
+    for (; n < nend; ++n) {
+        T acc_a = T(0), acc_b = T(0);
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            acc_a = fma(ta[k], wa[k], acc_a);
+            acc_b = fma(tb[k], wb[k], acc_b);
+        }
+        ya = fma(-__ldg(&ma[n]), ya, acc_a);
+        yb = fma(-__ldg(&mb[n]), yb, acc_b);
+#pragma unroll
+        for (int k = 0; k < W - 1; ++k) { wa[k] = wa[k + 1]; wb[k] = wb[k + 1]; }
+        const int pos = n + H + 1;
+        wa[W - 1] = pos < N ? sa[pos * P] : T(0);
+        wb[W - 1] = pos < N ? sb[pos * P] : T(0);
+        da[n * P] = ya;
+        db[n * P] = yb;
+    }
+    // rows N-H..N-1
+#pragma unroll
+    for (int b = 0; b < H; ++b) {
+        const int r = N - H + b;
+        ya = fma(-__ldg(&ma[r]), ya, pa[H + b]);
+        yb = fma(-__ldg(&mb[r]), yb, pb[H + b]);
+        da[r * P] = ya;
+        db[r * P] = yb;
+    }
+    // back substitution in chunks of kU, next chunk prefetched
+    const T *__restrict__ ca_ = oa.c;
+    const T *__restrict__ cb_ = ob.c;
+    const T *__restrict__ ia = oa.iw;
+    const T *__restrict__ ib = ob.iw;
+    T xa = ya * __ldg(&ia[N - 1]);
+    T xb = yb * __ldg(&ib[N - 1]);
+    da[(N - 1) * P] = xa;
+    db[(N - 1) * P] = xb;
+    const T xla = xa, xlb = xb;
+    n = N - 2;
+    T ya4[kU], yb4[kU], cA[kU], cB[kU], iA[kU], iB[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) {
+        const int r = max(n - j, 0);
+        ya4[j] = da[r * P]; yb4[j] = db[r * P];
+    }
+    load4(oa.cbk, cA); load4(ob.cbk, cB);
+    load4(oa.ibk, iA); load4(ob.ibk, iB);
+#pragma unroll 2
+    for (; n - kU + 1 >= 0; n -= kU) {
+        T y0a[kU], y0b[kU], c0a[kU], c0b[kU], i0a[kU], i0b[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            y0a[j] = ya4[j]; y0b[j] = yb4[j]; c0a[j] = cA[j]; c0b[j] = cB[j]; i0a[j] = iA[j]; i0b[j] = iB[j];
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            const int r = max(n - kU - j, 0);
+            ya4[j] = da[r * P]; yb4[j] = db[r * P];
+        }
+        const int kb = N - 2 - (n - kU);
+        load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+        load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            xa = fma(-c0a[j], xa, y0a[j]) * i0a[j];
+            xb = fma(-c0b[j], xb, y0b[j]) * i0b[j];
+            da[(n - j) * P] = xa;
+            db[(n - j) * P] = xb;
+        }
+    }
+    for (; n >= 0; --n) {
+        xa = fma(-__ldg(&ca_[n]), xa, da[n * P]) * __ldg(&ia[n]);
+        xb = fma(-__ldg(&cb_[n]), xb, db[n * P]) * __ldg(&ib[n]);
+        da[n * P] = xa;
+        db[n * P] = xb;
+    }
+    *fa = oa.periodic ? (T)((to_f64(xa) + oa.bog * to_f64(xla)) * oa.inv_den) : T(0);
+    *fb = ob.periodic ? (T)((to_f64(xb) + ob.bog * to_f64(xlb)) * ob.inv_den) : T(0);
+}
+
+// Corrected value of solution n of a line whose factor is f.
+template <typename T>
+__device__ __forceinline__ T corr(T x, T f, const LineOp<T> &op, int n) {
+    return op.periodic ? fma(-f, __ldg(&op.z[n]), x) : x;
+}
+
+// ---------------------------------------------------------------------
+// tile geometry
+// ---------------------------------------------------------------------
+struct Tile {
+    unsigned base;    // global index of (line 0, position 0)
+    unsigned sl, sn;  // strides between lines and along a line
+    int nlines;       // valid lines in this tile (<= L)
+    int N;            // line length
+    int ci, cj, ck;   // coordinates of (line 0, position 0)
+};
+
+template <int DIR>
+__device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
+    Tile t;
+    const unsigned nxy = (unsigned)g.Nx * (unsigned)g.Ny;
+    if (DIR == 0) {  // x-lines at rows j0.., plane k
+        int j0 = blockIdx.x * L, k = blockIdx.y;
+        t.base = (unsigned)k * nxy + (unsigned)j0 * g.Nx;
+        t.sl = g.Nx; t.sn = 1;
+        t.nlines = min(L, g.Ny - j0);
+        t.N = g.Nx;
+        t.ci = 0; t.cj = j0; t.ck = k;
+    } else if (DIR == 1) {  // y-lines at columns i0.., plane k
+        int i0 = blockIdx.x * L, k = blockIdx.y;
+        t.base = (unsigned)k * nxy + i0;
+        t.sl = 1; t.sn = g.Nx;
+        t.nlines = min(L, g.Nx - i0);
+        t.N = g.Ny;
+        t.ci = i0; t.cj = 0; t.ck = k;
+    } else {  // z-lines at columns i0.., row j
+        int i0 = blockIdx.x * L, j = blockIdx.y;
+        t.base = (unsigned)j * g.Nx + i0;
+        t.sl = 1; t.sn = nxy;
+        t.nlines = min(L, g.Nx - i0);
+        t.N = g.Nz;
+        t.ci = i0; t.cj = j; t.ck = 0;
+    }
+    return t;
+}
+
+// Point p of a tile: consecutive threads touch consecutive global addresses
+// (position-major for x-lines, line-major otherwise).  L is a power of two
+// (lgL its logarithm); division by the x-line length uses a precomputed
+// multiplier (divN: p / N = (umulhi(p, mul) + p) >> sh for p < 2^31).
+struct Pt {
+    unsigned gi;   // global index (a valid address even when !ok)
+    int o;         // shared-memory offset
+    int l, n;
+    bool ok;
+};
+
+template <int DIR>
+__device__ __forceinline__ Pt point(const Tile &t, int p, int L, int P, int lgL, FastDiv dv) {
+    Pt q;
+    if (DIR == 0) {
+        q.l = (int)((__umulhi((unsigned)p, dv.mul) + (unsigned)p) >> dv.sh);
+        q.n = p - q.l * t.N;
+    } else {
+        q.n = p >> lgL;
+        q.l = p & (L - 1);
+    }
+    q.ok = q.l < t.nlines && q.n < t.N;
+    q.gi = q.ok ? t.base + (unsigned)q.l * t.sl + (unsigned)q.n * t.sn : t.base;
+    q.o = q.n * P + q.l;
+    return q;
+}
+
+template <int DIR>
+__device__ __forceinline__ void coords(const Tile &t, int l, int n, int &i, int &j, int &k) {
+    if (DIR == 0) { i = n; j = t.cj + l; k = t.ck; }
+    else if (DIR == 1) { i = t.ci + l; j = n; k = t.ck; }
+    else { i = t.ci + l; j = t.cj; k = n; }
+}
+
+// ---------------------------------------------------------------------
+// shared-memory layout of a tile: per-line factors, then nbuf buffers
+// ---------------------------------------------------------------------
+template <typename T>
+struct Smem {
+    T *buf;
+    T *fact;  // [nbuf][L]
+    int bstride;
+    int P;
+    __device__ T *b(int k) const { return buf + (size_t)k * bstride; }
+};
+
+// Elements between consecutive buffers.  The solve tasks of one warp use
+// buffers two apart (A solves 0,2,4,..; B solves 1,3,5,..), each touching L
+// consecutive lines: a stride s with 2*s*e = L*e (mod 32 banks), e the
+// element size in 4-byte words, places the tasks of a warp on distinct banks.
+__host__ __device__ inline int buf_stride(int N, int P, int L, int e) {
+    const int mod = 16 / e;
+    const int want = (L / 2) % mod;
+    int st = N * P;
+    st += ((want - st % mod) + mod) % mod;
+    return st;
+}
+
+template <typename T>
+__device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<T> s;
+    s.P = P;
+    s.bstride = buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4));
+    s.fact = reinterpret_cast<T *>(smem_raw);
+    const int nf = (nbuf * L + 3) & ~3;
+    s.buf = reinterpret_cast<T *>(smem_raw) + nf;
+    return s;
+}
+
+// Per-thread loop over the points of a tile with a software pipeline: the
+// global loads of the thread's next point are issued before the current
+// point is computed, so memory latency overlaps the arithmetic.
+// ld(S&, p) loads point p; cp(S&) computes and stores it.
+template <typename S, typename LD, typename CP>
+__device__ __forceinline__ void pipelined(int NL, LD &&ld, CP &&cp) {
+    int p = threadIdx.x;
+    if (p >= NL) return;
+    S s0, s1;
+    ld(s0, p);
+    for (;;) {
+        const int p1 = p + blockDim.x;
+        if (p1 < NL) ld(s1, p1);
+        cp(s0);
+        if (p1 >= NL) break;
+        const int p2 = p1 + blockDim.x;
+        if (p2 < NL) ld(s0, p2);
+        cp(s1);
+        if (p2 >= NL) break;
+        p = p2;
+    }
+}
+
+// Per-thread loop over the points of a tile in batches of B: the loads of B
+// points are issued together, then the B points are computed and stored.
+template <typename S, int B, typename LD, typename CP>
+__device__ __forceinline__ void batched(int NL, LD &&ld, CP &&cp) {
+    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+        S s[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            const int p = p0 + b * blockDim.x;
+            ld(s[b], p < NL ? p : p0);
+            if (p >= NL) s[b].pt.ok = false;
+        }
+#pragma unroll
+        for (int b = 0; b < B; ++b) cp(s[b]);
+    }
+}
+
+// A task: solve A (src a, dst da, operator oa) and solve B, run together.
+// op: 0 = 1st derivative, 1 = 2nd derivative, 2 = filter.
+struct Task {
+    signed char a, da, oa, b, db, ob;
+};
+
+template <typename T, int H>
+__device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
+                                          const LineOp<T> &op0, const LineOp<T> &op1) {
+    for (int w = threadIdx.x; w < ntask * L; w += blockDim.x) {
+        const int t = w / L, l = w - t * L;
+        if (l >= nlines) continue;
+        const Task tk = tasks[t];
+        const LineOp<T> &oa = tk.oa == 1 ? op1 : op0;
+        const LineOp<T> &ob = tk.ob == 1 ? op1 : op0;
+        solve_pair<T, H>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
+                         sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T get(const Smem<T> &sm, int k, const Pt &p, int L, const LineOp<T> &op) {
+    return corr<T>(sm.b(k)[p.o], sm.fact[k * L + p.l], op, p.n);
+}
+
+// Sherman-Morrison vectors of the 1st and 2nd derivative at position n
+// (zero for wall lines), loaded once per point.
+template <typename T>
+struct Zn {
+    T z1, z2;
+};
+template <typename T>
+__device__ __forceinline__ Zn<T> zn(const LineOp<T> &d1, const LineOp<T> &d2, int n) {
+    Zn<T> z;
+    z.z1 = d1.periodic ? __ldg(&d1.z[n]) : T(0);
+    z.z2 = d2.periodic ? __ldg(&d2.z[n]) : T(0);
+    return z;
+}
+// Corrected solution of buffer k at point p, with z the operator's vector.
+template <typename T>
+__device__ __forceinline__ T gz(const Smem<T> &sm, int k, const Pt &p, int L, T z) {
+    return fma(-sm.fact[k * L + p.l], z, sm.b(k)[p.o]);
+}
+
+// ---------------------------------------------------------------------
+// primitives of one point (IdealGas.hpp:49-80)
+// ---------------------------------------------------------------------
+template <typename T>
+struct PrimW {
+    T ru, rv, rw, re, U, V, W, p, Tt;
+};
+
+template <typename T>
+__device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2, T r3, T r4) {
+    PrimW<T> s;
+    s.ru = r1; s.rv = r2; s.rw = r3; s.re = r4;
+    s.U = r1 / r0;
+    s.V = r2 / r0;
+    s.W = r3 / r0;
+    s.p = (T)gp.gm1 * (r4 - T(0.5) * r0 * (s.U * s.U + s.V * s.V + s.W * s.W));
+    s.Tt = s.p / (r0 * (T)gp.R);
+    return s;
+}
+
+}  // namespace cs3d

@@ -200,6 +200,38 @@ int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
  * requires CS3D_OPT_STORE_DIAGNOSTICS to have been on during that stage. */
 int cs3d_tgv_quantities(cs3d_handle *h, double out[7]);
 
+/* ---- discrete adjoint of the time steps --------------------------------
+ * No counterpart in the reference.  Gradient of an objective J of the state
+ * after n steps with respect to the state before them, by the transposed
+ * (discrete adjoint) step: filter^T, then the four RK4 stages in reverse,
+ * each J^T lam of the stage right-hand side through the transposed compact
+ * operators (D1^T = -D1, D2^T = D2, F^T = F on periodic grids), the
+ * generated pointwise adjoint of the flux and viscous terms and the chain
+ * rule through the ideal-gas primitives.  Scope: CS3D_FP64 handles with
+ * periodic boundaries, RK4 and a fixed time step (cfg.dt_fixed > 0).
+ *
+ * cs3d_adjoint_record runs n steps from the current state, keeping the state
+ * at every checkpoint_every-th step (0: ceil(sqrt(n))); memory is
+ * (n/checkpoint_every + checkpoint_every) states plus a workspace of about
+ * 150 fields.  cs3d_adjoint_backward replays each segment from its
+ * checkpoint, recomputes the stage inputs of every step and takes the steps
+ * back; it writes dJ/dq0 to grad (5*npts, field-major rho, rhoU, rhoV, rhoW,
+ * rhoE) and returns the solver to the recorded final state.  objective
+ * CS3D_ADJ_KE_MEAN: J = mean over points of rho |u|^2 / 2 of the final
+ * state (returned in *J); CS3D_ADJ_SEED: seed = dJ/dq of the final state
+ * (5*npts host doubles). */
+#define CS3D_ADJ_SEED     0
+#define CS3D_ADJ_KE_MEAN  1
+int cs3d_adjoint_record(cs3d_handle *h, int nsteps, int checkpoint_every);
+int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double *seed, double *grad, double *J);
+
+/* Building blocks of the adjoint, on a state q given on the host (5*npts):
+ * R(q), the stage right-hand side evaluated from its 48 pointwise inputs
+ * (unfused: primitives, fluxes and derivative fields stored, then combined),
+ * and out = (dR/dq)^T lam. */
+int cs3d_rhs_eval(cs3d_handle *h, const double *q, double *R);
+int cs3d_rhs_vjp(cs3d_handle *h, const double *q, const double *lam, double *out);
+
 /* ---- allocation-free kinetic energy -------------------------------------
  * No counterpart in the reference.  The KEsum column of
  * cs3d_tgv_quantities (sum over points of rho |u|^2 / 2, CSolver_AWS.cpp:

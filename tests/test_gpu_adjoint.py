@@ -1,0 +1,153 @@
+"""The discrete adjoint through the C ABI, against finite differences of the
+FP64 forward (the same product path, fixed time step).
+
+* R(q) evaluated from the stored pointwise inputs equals the fused stage's
+  right-hand side (dq/dt of stage 1);
+* <w, J v> by central differences of R equals <J^T w, v> (adjoint test of
+  one stage, random noise in every field);
+* the gradient of the final mean kinetic energy with respect to the initial
+  velocity equals central differences of the forward on seeded random
+  directions, filtered every step and every second step;
+* the checkpoint interval does not change the gradient, and the solver is
+  back at its recorded final state afterwards.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tgv_fixed_dt(gpu_pkg, cases, N, **kw):
+    cfg, ic = cases.tgv(N, **kw)
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.step()
+    dt = s.scalars()[0]
+    s.close()
+    cfg.dt_fixed = dt
+    return cfg, ic
+
+
+def _state(gpu_pkg, cases, N=16, steps=3, seed=0):
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
+    rng = np.random.default_rng(seed)
+    rho0, p0, U0, V0, W0 = ic
+    W0 = 0.1 * np.sin(np.arange(N)[:, None, None] * 2 * np.pi / N + rng.uniform(0, 6.28)) * np.ones_like(U0)
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(rho0, p0 * (1 + 0.01 * rng.standard_normal(U0.shape)), U0, V0, W0)
+    s.run(steps)
+    return s, cfg, s.conserved()
+
+
+def test_rhs_eval_matches_fused_stage(gpu_pkg, cases):
+    s, cfg, q = _state(gpu_pkg, cases)
+    R = s.rhs_eval(q)
+    s.set_option(gpu_pkg.OPT_STORE_INCREMENTS, 1)
+    s.pre_step()
+    s.sub_step(1, 0)
+    dt = s.scalars()[0]
+    dq = np.stack([s.get(15 + f) for f in range(5)])
+    for f in range(5):
+        scale = np.abs(dq[f]).max()
+        assert np.abs(dt * R[f] - dq[f]).max() <= 1e-11 * scale, f
+
+
+def test_rhs_vjp_adjoint_identity(gpu_pkg, cases):
+    s, cfg, q = _state(gpu_pkg, cases, seed=1)
+    rng = np.random.default_rng(7)
+    scale = np.abs(q).reshape(5, -1).max(axis=1)[:, None, None, None]
+    v = 1e-2 * scale * rng.standard_normal(q.shape)
+    w = rng.standard_normal(q.shape)
+    eps = 1e-4
+    jv = (s.rhs_eval(q + eps * v) - s.rhs_eval(q - eps * v)) / (2 * eps)
+    lhs = float(np.sum(w * jv))
+    rhs = float(np.sum(s.rhs_vjp(q, w) * v))
+    assert abs(lhs - rhs) <= 1e-7 * abs(lhs), (lhs, rhs)
+
+
+def _mean_ke(q):
+    return float(np.mean(0.5 * (q[1] ** 2 + q[2] ** 2 + q[3] ** 2) / q[0]))
+
+
+def _forward_J(gpu_pkg, cfg, ic, nsteps):
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.run(nsteps)
+    J = _mean_ke(s.conserved())
+    s.close()
+    return J
+
+
+@pytest.mark.parametrize("filter_step,every", [(1, 4), (2, 0)])
+def test_adjoint_matches_finite_differences(gpu_pkg, cases, filter_step, every):
+    N, nsteps = 16, 6
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=filter_step)
+    rho0, p0, U0, V0, W0 = ic
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.adjoint_record(nsteps, every)
+    qN = s.conserved()
+    grad, J = s.adjoint_backward(gpu_pkg.ADJ_KE_MEAN)
+    assert abs(J - _mean_ke(qN)) <= 1e-14 * J
+    gU, gV, gW = gpu_pkg.ic_velocity_gradient(grad, rho0, U0, V0, W0)
+    rng = np.random.default_rng(100 + filter_step)
+    eps = 1e-5
+    for d in range(3):
+        dU, dV, dW = (rng.standard_normal(U0.shape) for _ in range(3))
+        adj = float(np.sum(gU * dU + gV * dV + gW * dW))
+        Jp = _forward_J(gpu_pkg, cfg, (rho0, p0, U0 + eps * dU, V0 + eps * dV, W0 + eps * dW), nsteps)
+        Jm = _forward_J(gpu_pkg, cfg, (rho0, p0, U0 - eps * dU, V0 - eps * dV, W0 - eps * dW), nsteps)
+        fd = (Jp - Jm) / (2 * eps)
+        assert abs(adj - fd) <= 1e-6 * abs(fd), (d, adj, fd)
+
+
+def test_adjoint_checkpointing_and_restore(gpu_pkg, cases):
+    N, nsteps = 16, 5
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
+    grads = []
+    for every in (1, 2, 5):
+        s = gpu_pkg.Solver(cfg)
+        s.set_initial_conditions(*ic)
+        s.adjoint_record(nsteps, every)
+        qN = s.conserved()
+        g, _ = s.adjoint_backward(gpu_pkg.ADJ_KE_MEAN)
+        grads.append(g)
+        assert np.array_equal(s.conserved(), qN)
+        assert s.scalars()[2] == nsteps
+        s.step()
+        ref = gpu_pkg.Solver(cfg)
+        ref.set_initial_conditions(*ic)
+        ref.run(nsteps + 1)
+        assert np.array_equal(s.conserved(), ref.conserved())
+    assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
+
+
+def test_adjoint_user_seed_is_linear(gpu_pkg, cases):
+    N, nsteps = 12, 3
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.adjoint_record(nsteps)
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((5, N, N, N))
+    b = rng.standard_normal((5, N, N, N))
+    ga, _ = s.adjoint_backward(gpu_pkg.ADJ_SEED, a)
+    gb, _ = s.adjoint_backward(gpu_pkg.ADJ_SEED, b)
+    gab, _ = s.adjoint_backward(gpu_pkg.ADJ_SEED, 2.0 * a - b)
+    assert np.abs(gab - (2.0 * ga - gb)).max() <= 1e-10 * np.abs(gab).max()
+
+
+def test_adjoint_rejects_unsupported(gpu_pkg, cases):
+    cfg, ic = cases.tgv(16)  # no fixed time step
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    with pytest.raises(gpu_pkg.CS3DError) as e:
+        s.adjoint_record(2)
+    assert e.value.code == 6
+    cfg, ic = cases.wall_box()
+    cfg.dt_fixed = 1e-3
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    with pytest.raises(gpu_pkg.CS3DError) as e:
+        s.adjoint_record(2)
+    assert e.value.code == 6
