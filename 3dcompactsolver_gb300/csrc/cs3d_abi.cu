@@ -1224,7 +1224,7 @@ static int adj_check(cs3d_handle *h) {
         if (h->cfg.bc_type[d] != CS3D_PERIODIC_SOLVE)
             return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only (direction %d)", d);
     if (h->sponge || h->wall_faces) return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only");
-    if (h->mixed) return fail(CS3D_ERR_STATE, "the adjoint runs on CS3D_FP64 handles");
+    if (h->cfg.rk != CS3D_RK4) return fail(CS3D_ERR_STATE, "the adjoint is built for RK4");
     return CS3D_OK;
 }
 
@@ -1425,21 +1425,39 @@ static void filter_order(int fts, int order[3]) {
     else { order[0] = 2; order[1] = 0; order[2] = 1; }
 }
 
+// The solver's state q1 := q (and, in the mixed form, its FP32 shadow).
+static int adj_set_state(cs3d_handle *h, double *const q[5]) {
+    int rc = copy5(h, h->q1.f, q);
+    if (rc) return rc;
+    return h->mixed ? launch_shadow_of(h, h->q1, h->q1s) : CS3D_OK;
+}
+
 // Adjoint of one time step taken from the state q0 with counters (ts, fts):
 // adj_f[ADJ_QB] holds dJ/dq after the step on entry and dJ/dq0 on return.
+// T is the work type: the stage Jacobians are transposed in T at the stage
+// inputs the forward used (FP64 q1, qk; or, in the mixed form, the FP32
+// shadows q1s, qks); the adjoint state and the filter transpose stay FP64.
+template <typename T>
 static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     int rc;
     double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
     double **QB = h->adj_f[ADJ_QB], **QB2 = h->adj_f[ADJ_QB2], **LAM = h->adj_f[ADJ_LAM];
     double **YS = h->adj_f[ADJ_YS], **YT = h->adj_f[ADJ_YT];
-    // stage inputs y2, y3, y4 of the forward step
+    const size_t n = (size_t)h->g.npts;
+    // stage inputs y1 = q0, y2, y3, y4 of the forward step, in T
+    const T *yin[4][5];
     h->timeStep = ts;
     h->filterTimeStep = fts;
-    if ((rc = copy5(h, h->q1.f, q0))) return rc;
+    if ((rc = adj_set_state(h, q0))) return rc;
+    for (int f = 0; f < 5; f++) yin[0][f] = sizeof(T) == 8 ? (const T *)q0[f] : (const T *)h->q1s[f];
     if ((rc = cs3d_pre_step(h))) return rc;
     for (int st = 1; st <= 3; st++) {
-        if ((rc = run_stage<double>(h, st, 0))) return rc;
-        if ((rc = copy5(h, Y[st - 1], h->qk.f))) return rc;
+        if ((rc = run_stage<T>(h, st, 0))) return rc;
+        for (int f = 0; f < 5; f++) {
+            const void *src = sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f];
+            CS3D_CUDA(cudaMemcpyAsync(Y[st - 1][f], src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+            yin[st][f] = (const T *)Y[st - 1][f];
+        }
     }
     const bool filtered = h->timeStep % h->cfg.filter_step == 0;
     const double dt = h->cfg.dt_fixed;
@@ -1463,13 +1481,12 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     // y2 = q + dt/2 k1, y3 = q + dt/2 k2, y4 = q + dt k3, k_s = R(y_s)
     const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};  // weight of k_s in q+
     const double cb[4] = {dt / 2.0, dt / 2.0, dt, 0.0};             // weight of k_s in y_{s+1}
-    double *const *yin[4] = {q0, Y[0], Y[1], Y[2]};
     for (int s = 3; s >= 0; s--) {
         // lam_s = ca_s qbar+ + cb_s ybar_{s+1}
         if (s == 3) rc = adj_lin(h, LAM, ca[s], QB2, 0.0, nullptr);
         else rc = adj_lin(h, LAM, ca[s], QB2, cb[s], YT);
         if (rc) return rc;
-        if ((rc = adj_rhs_vjp<double>(h, yin[s], LAM, YT))) return rc;
+        if ((rc = adj_rhs_vjp<T>(h, yin[s], LAM, YT))) return rc;
         if (s == 3) rc = copy5(h, YS, YT);
         else rc = adj_lin(h, YS, 1.0, YS, 1.0, YT);
         if (rc) return rc;
@@ -1481,7 +1498,6 @@ extern "C" int cs3d_adjoint_record(cs3d_handle *h, int nsteps, int checkpoint_ev
     int rc = adj_check(h);
     if (rc) return rc;
     if (!(h->cfg.dt_fixed > 0.0)) return fail(CS3D_ERR_STATE, "the adjoint needs a fixed time step (cfg.dt_fixed > 0)");
-    if (h->cfg.rk != CS3D_RK4) return fail(CS3D_ERR_STATE, "the adjoint is built for RK4");
     if (nsteps < 1) return fail(CS3D_ERR_ARG, "nsteps = %d", nsteps);
     if (checkpoint_every < 0) return fail(CS3D_ERR_ARG, "checkpoint_every = %d", checkpoint_every);
     DeviceGuard dg(h->dev);
@@ -1579,7 +1595,7 @@ extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double
                 double *cur[5], *nxt[5];
                 slab5(h, h->adj_seg + (size_t)j * 5 * n, cur);
                 slab5(h, h->adj_seg + (size_t)(j + 1) * 5 * n, nxt);
-                if ((rc = copy5(h, h->q1.f, cur))) return rc;
+                if ((rc = adj_set_state(h, cur))) return rc;
                 if ((rc = cs3d_step(h))) return rc;
                 if ((rc = copy5(h, nxt, h->q1.f))) return rc;
             }
@@ -1587,13 +1603,14 @@ extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double
         for (int j = m - 1; j >= 0; j--) {
             double *cur[5];
             slab5(h, h->adj_seg + (size_t)j * 5 * n, cur);
-            if ((rc = adj_step(h, tsv[j], ftsv[j], cur))) return rc;
+            rc = h->mixed ? adj_step<float>(h, tsv[j], ftsv[j], cur) : adj_step<double>(h, tsv[j], ftsv[j], cur);
+            if (rc) return rc;
         }
     }
     for (int f = 0; f < 5; f++)
         CS3D_CUDA(cudaMemcpyAsync(grad_host + (size_t)f * n, QB[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
     // back to the recorded final state
-    if ((rc = copy5(h, h->q1.f, FIN))) return rc;
+    if ((rc = adj_set_state(h, FIN))) return rc;
     h->timeStep = h->adj_end_ts;
     h->filterTimeStep = h->adj_end_fts;
     CS3D_CUDA(cudaMemcpyAsync(h->scal, h->adj_end_scal, 2 * 8, cudaMemcpyHostToDevice, h->stream));
@@ -1610,6 +1627,39 @@ static int adj_upload_state(cs3d_handle *h, const double *q_host, double *const 
     return CS3D_OK;
 }
 
+// FP32 copy of five FP64 fields, in the ADJ_Y3 group's storage
+static int adj_narrow(cs3d_handle *h, double *const q[5], float *out[5]) {
+    Q5 src{};
+    for (int f = 0; f < 5; f++) {
+        src.f[f] = q[f];
+        out[f] = (float *)h->adj_f[ADJ_Y3][f];
+    }
+    return launch_shadow_of(h, src, out);
+}
+
+template <typename T>
+static int adj_rhs_eval(cs3d_handle *h, double *const Q[5], double *const R[5]) {
+    const T *qin[5];
+    int rc;
+    if (sizeof(T) == 4) {
+        float *qs[5];
+        if ((rc = adj_narrow(h, Q, qs))) return rc;
+        for (int f = 0; f < 5; f++) qin[f] = (const T *)qs[f];
+    } else {
+        for (int f = 0; f < 5; f++) qin[f] = (const T *)Q[f];
+    }
+    if ((rc = adj_tape<T>(h, qin))) return rc;
+    RhsEvalArgs<T> ra{};
+    ra.g = h->g;
+    ra.gas = h->gas;
+    for (int i = 0; i < 48; i++) ra.tape[i] = (const T *)h->adj_tape[i];
+    for (int f = 0; f < 5; f++) ra.R[f] = R[f];
+    tstart(h, CS3D_K_OTHER);
+    CS3D_CUDA(launch_rhs_eval<T>(ra, h->stream));
+    tend(h);
+    return CS3D_OK;
+}
+
 extern "C" int cs3d_rhs_eval(cs3d_handle *h, const double *q_host, double *R_host) {
     int rc = adj_check(h);
     if (rc) return rc;
@@ -1618,15 +1668,8 @@ extern "C" int cs3d_rhs_eval(cs3d_handle *h, const double *q_host, double *R_hos
     if ((rc = adj_workspace(h))) return rc;
     double **Q = h->adj_f[ADJ_Y2], **R = h->adj_f[ADJ_YT];
     if ((rc = adj_upload_state(h, q_host, Q))) return rc;
-    if ((rc = adj_tape<double>(h, Q))) return rc;
-    RhsEvalArgs<double> ra{};
-    ra.g = h->g;
-    ra.gas = h->gas;
-    for (int i = 0; i < 48; i++) ra.tape[i] = (const double *)h->adj_tape[i];
-    for (int f = 0; f < 5; f++) ra.R[f] = R[f];
-    tstart(h, CS3D_K_OTHER);
-    CS3D_CUDA(launch_rhs_eval<double>(ra, h->stream));
-    tend(h);
+    rc = h->mixed ? adj_rhs_eval<float>(h, Q, R) : adj_rhs_eval<double>(h, Q, R);
+    if (rc) return rc;
     const size_t n = (size_t)h->g.npts;
     for (int f = 0; f < 5; f++)
         CS3D_CUDA(cudaMemcpyAsync(R_host + (size_t)f * n, R[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
@@ -1643,7 +1686,14 @@ extern "C" int cs3d_rhs_vjp(cs3d_handle *h, const double *q_host, const double *
     double **Q = h->adj_f[ADJ_Y2], **LAM = h->adj_f[ADJ_LAM], **OUT = h->adj_f[ADJ_YT];
     if ((rc = adj_upload_state(h, q_host, Q))) return rc;
     if ((rc = adj_upload_state(h, lam_host, LAM))) return rc;
-    if ((rc = adj_rhs_vjp<double>(h, Q, LAM, OUT))) return rc;
+    if (h->mixed) {
+        float *qs[5];
+        if ((rc = adj_narrow(h, Q, qs))) return rc;
+        rc = adj_rhs_vjp<float>(h, qs, LAM, OUT);
+    } else {
+        rc = adj_rhs_vjp<double>(h, Q, LAM, OUT);
+    }
+    if (rc) return rc;
     const size_t n = (size_t)h->g.npts;
     for (int f = 0; f < 5; f++)
         CS3D_CUDA(cudaMemcpyAsync(out_host + (size_t)f * n, OUT[f], n * 8, cudaMemcpyDeviceToHost, h->stream));

@@ -207,8 +207,11 @@ int cs3d_tgv_quantities(cs3d_handle *h, double out[7]);
  * each J^T lam of the stage right-hand side through the transposed compact
  * operators (D1^T = -D1, D2^T = D2, F^T = F on periodic grids), the
  * generated pointwise adjoint of the flux and viscous terms and the chain
- * rule through the ideal-gas primitives.  Scope: CS3D_FP64 handles with
- * periodic boundaries, RK4 and a fixed time step (cfg.dt_fixed > 0).
+ * rule through the ideal-gas primitives.  Scope: periodic boundaries, RK4
+ * and a fixed time step (cfg.dt_fixed > 0).  On a CS3D_FP64 handle every
+ * operation is FP64; on a CS3D_FP32_MIXED handle the stage Jacobians are
+ * transposed in FP32 at the FP32 stage inputs of the mixed forward, while
+ * the adjoint state, the RK combination and the filter transpose are FP64.
  *
  * cs3d_adjoint_record runs n steps from the current state, keeping the state
  * at every checkpoint_every-th step (0: ceil(sqrt(n))); memory is

@@ -151,3 +151,44 @@ def test_adjoint_rejects_unsupported(gpu_pkg, cases):
     with pytest.raises(gpu_pkg.CS3DError) as e:
         s.adjoint_record(2)
     assert e.value.code == 6
+
+
+def test_mixed_adjoint_tracks_fp64(gpu_pkg, cases):
+    """The FP32-mixed adjoint (FP32 stage Jacobians at the mixed forward's
+    stage inputs) against the FP64 adjoint and FP64 finite differences."""
+    N, nsteps = 24, 8
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
+    cfg_m, _ = cases.tgv(N, precision=gpu_pkg.FP32_MIXED)
+    cfg_m.dt_fixed = cfg.dt_fixed
+    grads = []
+    for c in (cfg, cfg_m):
+        s = gpu_pkg.Solver(c)
+        s.set_initial_conditions(*ic)
+        s.adjoint_record(nsteps, 3)
+        g, _ = s.adjoint_backward(gpu_pkg.ADJ_KE_MEAN)
+        grads.append(gpu_pkg.ic_velocity_gradient(g, ic[0], ic[2], ic[3], ic[4]))
+        s.close()
+    num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(grads[1], grads[0])))
+    den = np.sqrt(sum(np.sum(b * b) for b in grads[0]))
+    assert num / den <= 1e-4, num / den
+    rng = np.random.default_rng(11)
+    rho0, p0, U0, V0, W0 = ic
+    eps = 1e-5
+    dU, dV, dW = (rng.standard_normal(U0.shape) for _ in range(3))
+    fd = (_forward_J(gpu_pkg, cfg, (rho0, p0, U0 + eps * dU, V0 + eps * dV, W0 + eps * dW), nsteps)
+          - _forward_J(gpu_pkg, cfg, (rho0, p0, U0 - eps * dU, V0 - eps * dV, W0 - eps * dW), nsteps)) / (2 * eps)
+    am = float(np.sum(grads[1][0] * dU + grads[1][1] * dV + grads[1][2] * dW))
+    assert abs(am - fd) <= 1e-4 * abs(fd), (am, fd)
+
+
+def test_mixed_rhs_vjp_tracks_fp64(gpu_pkg, cases):
+    s, cfg, q = _state(gpu_pkg, cases, seed=2)
+    cfg_m, _ = cases.tgv(16, precision=gpu_pkg.FP32_MIXED)
+    m = gpu_pkg.Solver(cfg_m)
+    m.set_initial_conditions(*[np.ones((16, 16, 16))] * 2 + [np.zeros((16, 16, 16))] * 3)
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal(q.shape)
+    a = s.rhs_vjp(q, w)
+    b = m.rhs_vjp(q, w)
+    for f in range(5):
+        assert np.abs(a[f] - b[f]).max() <= 2e-3 * np.abs(a[f]).max(), f
