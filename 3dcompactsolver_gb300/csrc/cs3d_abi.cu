@@ -53,6 +53,7 @@ namespace {
 
 struct HostOp {
     std::vector<double> m, iw, c, z;
+    std::vector<double> alo, aup;  // off-diagonals of A (unit diagonal), before any cyclic modification
     double taps[kTaps] = {0};
     double btaps[2 * kMaxH][kTaps] = {{0}};
     int boff[2 * kMaxH] = {0};
@@ -176,6 +177,8 @@ HostOp make_op(int kind, int N, int bc, double dh, double alphaF) {
             }
         }
     }
+    op.alo = lo;
+    op.aup = up;
     // Thomas factors of the (possibly corner-modified) matrix
     op.m.assign(N, 0.0);
     op.iw.assign(N, 0.0);
@@ -188,6 +191,28 @@ HostOp make_op(int kind, int N, int bc, double dh, double alphaF) {
     for (int i = 0; i < N; i++) op.iw[i] = 1.0 / w[i];
     if (!op.periodic) op.z.assign(N, 0.0);
     return op;
+}
+
+// The filter's correction operator F - I = A^-1 (B - A): the same left-hand
+// side, right-hand-side rows B - A.  Its taps are small and sum to zero, so in
+// FP32 the rounding of the coefficients changes only the (small) correction
+// and not the gain of the filter at the energy-carrying wavenumbers, which
+// the FP32 form of F itself would (a drift of the kinetic energy by about
+// 1e-8 per filter pass).
+HostOp make_filter_correction(const HostOp &F) {
+    HostOp d = F;
+    const int H = F.H, N = F.N;
+    d.taps[kMaxH] -= 1.0;  // interior rows of A: alpha, 1, alpha
+    d.taps[kMaxH - 1] -= F.alo[N / 2];
+    d.taps[kMaxH + 1] -= F.aup[N / 2];
+    for (int b = 0; b < 2 * H; b++) {
+        const int row = b < H ? b : N - 2 * H + b;
+        const int col = row - F.boff[b];  // the row's own position among its taps
+        d.btaps[b][col] -= 1.0;
+        if (col > 0) d.btaps[b][col - 1] -= F.alo[row];
+        if (col + 1 < kTaps) d.btaps[b][col + 1] -= F.aup[row];
+    }
+    return d;
 }
 
 // Device copy of an operator in precision T.
@@ -294,6 +319,7 @@ struct cs3d_handle {
     // operators: [dir][kind-1]
     DevOp<double> op64[3][3];
     DevOp<float> op32[3][3];
+    DevOp<float> op32fc[3];  // FP32 filter correction F - I (mixed form)
     // tiles
     int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads = 128;
     // step state
@@ -575,11 +601,12 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             HostOp ho = make_op(k, Nd[d], cfg->bc_type[d], dd[d], cfg->alphaF);
             int r = upload_op<double>(ho, h->op64[d][k - 1], h->stream);
             if (!r) r = upload_op<float>(ho, h->op32[d][k - 1], h->stream);
+            if (!r && k == 3) r = upload_op<float>(make_filter_correction(ho), h->op32fc[d], h->stream);
             if (r) return fail_free(r);
         }
     for (int d = 0; d < 3; d++) {
         h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
-        h->Lf[d] = pick_L(h->tb, 5, Nd[d], d == 0 ? 1 : 0);
+        h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0);
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
@@ -604,6 +631,8 @@ extern "C" int cs3d_destroy(cs3d_handle *h) {
             if (h->op64[d][k].mem) cudaFree(h->op64[d][k].mem);
             if (h->op32[d][k].mem) cudaFree(h->op32[d][k].mem);
         }
+    for (int d = 0; d < 3; d++)
+        if (h->op32fc[d].mem) cudaFree(h->op32fc[d].mem);
     if (h->dq[0]) for (int f = 0; f < 5; f++) cudaFree(h->dq[f]);
     if (h->diag[0]) for (int f = 0; f < 3; f++) cudaFree(h->diag[f]);
     if (h->prim_out) cudaFree(h->prim_out);
@@ -841,7 +870,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                 fa.P = h->Lf[d] + (d == 0 ? 1 : 0);
                 fa.threads = h->threads;
                 if (sizeof(T) == 8) fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][2].op);
-                else fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op32[d][2].op);
+                else fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op32fc[d].op);
                 void **src = pass == 1 ? h->ft1 : h->ft2;
                 void **dst = pass == 0 ? h->ft1 : h->ft2;
                 for (int f = 0; f < 5; f++) {

@@ -418,19 +418,23 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_z
 // ---------------------------------------------------------------------
 // compact filter, one direction, five fields (Filter.cpp:98-171)
 // ---------------------------------------------------------------------
-// Plain form: FP64 in, FP64 out.  Mixed form: the first pass reads FP64 q2
-// minus a per-field reference value (the field's initial mean, so the FP32
-// numbers are fluctuations), the middle pass works in FP32, and the last pass
-// writes q1 = q2 + (filtered - unfiltered) in FP64 plus q1's FP32 shadow.
+// Plain form: FP64 in, FP64 out, a.op = F.  Mixed form: a.op is the
+// correction F - I, solved out of place (buffers 5..9), and the pass writes
+// v + (F - I) v; the first pass reads FP64 q2 minus a per-field reference
+// value (the field's initial mean, so the FP32 numbers are fluctuations), the
+// middle pass works in FP32, and the last pass writes
+// q1 = q2 + (filtered - unfiltered) in FP64 plus q1's FP32 shadow.
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
+__constant__ Task kTasksFc[3] = {{0, 5, 2, 1, 6, 2}, {2, 7, 2, 3, 8, 2}, {4, 9, 2, 4, 9, 2}};
 
 template <typename T, int DIR>
 __global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
     constexpr int B = 2;
+    constexpr bool kCorr = sizeof(T) == 4;
     const int L = a.L, P = a.P;
     const Tile t = make_tile<DIR>(a.g, L);
     const int N = t.N, NL = N * L;
-    Smem<T> sm = smem_layout<T>(5, L, P, N);
+    Smem<T> sm = smem_layout<T>(kCorr ? 10 : 5, L, P, N);
     for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
         Pt pt[B];
         T v[B][5];
@@ -450,7 +454,7 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
         }
     }
     __syncthreads();
-    run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
+    run_tasks<T, 4>(sm, kCorr ? kTasksFc : kTasksF, 3, L, t.nlines, a.op, a.op);
     __syncthreads();
     for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
         Pt pt[B];
@@ -467,7 +471,7 @@ __global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
             const unsigned gi = pt[b].gi;
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
-                const T v = get(sm, f, pt[b], L, a.op);
+                const T v = kCorr ? sm.b(f)[pt[b].o] + get(sm, 5 + f, pt[b], L, a.op) : get(sm, f, pt[b], L, a.op);
                 if (a.dst64.f[f]) {
                     double nv;
                     if (a.delta_from.f[f]) {
@@ -558,7 +562,7 @@ cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s) {
 template <typename T>
 cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s) {
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
-    const size_t sm = tile_smem<T>(5, a.L, a.P, N);
+    const size_t sm = tile_smem<T>(sizeof(T) == 4 ? 10 : 5, a.L, a.P, N);
     const dim3 grid = tile_grid(dir, a.g, a.L);
     if (dir == 0) return launch_tile_kernel(k_filter<T, 0>, a, grid, sm, s);
     if (dir == 1) return launch_tile_kernel(k_filter<T, 1>, a, grid, sm, s);
