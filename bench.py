@@ -84,7 +84,7 @@ def make_workload(name, precision):
         desc = "decaying isotropic turbulence 256^3, RK4, Mt 0.3, E(k)~(k/8)^4 exp(-2(k/8)^2), seed 0"
     elif name == "shear":
         cfg, ic = c.shear_layer(256, 128, 42, precision=prec)
-        desc = "temporal shear layer 256x128x42, TVD-RK3, y walls + 15% sponge, Mach 0.3, seed 0"
+        desc = "temporal shear layer 256x128x42, TVD-RK3, y walls + 15% sponge band, du 0.6 (Mach 0.3), mu_ref 0.00375, filter every 5 steps, seed 0"
     else:
         raise SystemExit(f"unknown workload {name}")
     return cfg, ic, desc
