@@ -382,6 +382,32 @@ def run_ours(args):
         s2.close()
         s3.close()
 
+    # the discrete adjoint of the same workload (periodic RK4 only): record
+    # `steps` steps at the current dt frozen, then the backward sweep
+    adjoint = None
+    if not args.no_adjoint and cfg.rk == 0 and all(int(b) == 0 for b in cfg.bc_type):
+        cfga, ica, _ = make_workload(args.workload, args.precision)
+        cfga.dt_fixed = s.scalars()[0]
+        sa = pkg.Solver(cfga)
+        sa.set_initial_conditions(*ica)
+        sa.sync()
+        t0 = time.perf_counter()
+        sa.adjoint_record(args.steps)
+        sa.sync()
+        t1 = time.perf_counter()
+        _, J = sa.adjoint_backward(pkg.ADJ_KE_MEAN)
+        t2 = time.perf_counter()
+        sa.close()
+        back_s = _barrier_max(t2 - t1, ws)
+        adjoint = {"objective": "mean KE of the final state", "steps": args.steps,
+                   "checkpoint_every": int(math.ceil(math.sqrt(args.steps))),
+                   "record_ms_per_step": round((t1 - t0) * 1e3 / args.steps, 3),
+                   "backward_ms_per_step": round(back_s * 1e3 / args.steps, 3),
+                   "backward_over_forward": round(back_s * 1e3 / ms, 2),
+                   "value": round(ws * npts * args.steps / back_s / 1e6, 3),
+                   "unit": "Mpts x steps / s (backward sweep)",
+                   "check": "profiles/adjoint_tgv128.md (16 directions vs central differences)"}
+
     cb = cpu_baseline(args.workload) if (rank == 0 and ws == 1 and not args.no_cpu) else None
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
@@ -398,6 +424,8 @@ def run_ours(args):
                     "d2h_bytes_per_step": 5 * 8 * npts},
             "gpu_launches": int(launches)}
     line.update(other)
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     s.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -417,6 +445,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the other form and the KE error")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint timing")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
