@@ -610,10 +610,10 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
-    h->threads = 128;
+    h->threads = h->mixed ? sweep_threads<float>() : sweep_threads<double>();
     if (const char *e = getenv("CS3D_THREADS")) {
         long v = strtol(e, nullptr, 10);
-        if (v == 64 || v == 128) h->threads = (int)v;
+        if (v == 64 || v == 128 || (v <= h->threads && v % 32 == 0 && v > 0)) h->threads = (int)v;
     }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
@@ -868,7 +868,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                 fa.lgL = ilog2(h->Lf[d]);
                 fa.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
                 fa.P = h->Lf[d] + (d == 0 ? 1 : 0);
-                fa.threads = h->threads;
+                fa.threads = 128;
                 if (sizeof(T) == 8) fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][2].op);
                 else fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op32fc[d].op);
                 void **src = pass == 1 ? h->ft1 : h->ft2;

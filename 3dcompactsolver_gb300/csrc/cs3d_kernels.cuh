@@ -2,7 +2,16 @@
 #pragma once
 #include "cs3d_dev.cuh"
 
+#ifndef CS3D_TPB
+#define CS3D_TPB 256  // threads per block of the mixed-form stage sweeps
+#endif
+
 namespace cs3d {
+
+// threads per block of the stage sweeps in work type T (the plain FP64 form
+// needs up to 255 registers per thread and runs 128)
+template <typename T>
+__host__ __device__ constexpr int sweep_threads() { return sizeof(T) == 4 ? CS3D_TPB : 128; }
 
 // Ideal-gas constants (IdealGas.hpp:36-46).
 struct GasParams {

@@ -38,8 +38,17 @@
 #ifndef CS3D_ZBC
 #define CS3D_ZBC 2     // points per thread in flight in the z sweep's consume phase
 #endif
-#ifndef CS3D_MINB
-#define CS3D_MINB 3    // resident blocks per SM the mixed-form sweeps are compiled for
+// Resident blocks per SM the mixed-form sweeps are compiled for (256 threads
+// each: x at 3 blocks / 80 registers, y and z at 2 blocks / 128 registers
+// were fastest at 128^3); the plain form runs 128 threads, 2 blocks.
+#ifndef CS3D_MINB_X
+#define CS3D_MINB_X 3
+#endif
+#ifndef CS3D_MINB_Y
+#define CS3D_MINB_Y 2
+#endif
+#ifndef CS3D_MINB_Z
+#define CS3D_MINB_Z 2
 #endif
 
 namespace cs3d {
@@ -53,7 +62,7 @@ __constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}
                                 {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_x(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -145,7 +154,7 @@ __constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}
                                 {YF4, YF4, 0, YF4, YF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_y(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -231,7 +240,7 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? CS3D_MINB : 2) k_sweep_z(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<2>(a.g, L);
     const int N = t.N, NL = N * L;
