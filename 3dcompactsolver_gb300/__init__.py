@@ -74,6 +74,8 @@ def lib():
         for name in ("cs3d_deriv1", "cs3d_deriv2", "cs3d_filter"):
             getattr(L, name).argtypes = [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.cs3d_tgv_quantities.argtypes = [_H, _DP]
+        L.cs3d_turbulence_quantities.argtypes = [_H, _DP]
+        L.cs3d_shear_layer_info.argtypes = [_H, _DP]
         L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
                                         ctypes.c_int]
         L.cs3d_version.argtypes = [ctypes.POINTER(ctypes.c_int)] * 3
@@ -222,6 +224,18 @@ class Solver:
         sp = _dptr(keep) if keep is not None else None
         check(lib().cs3d_adjoint_backward(self.h, int(objective), sp, _dptr(grad), ctypes.byref(J)))
         return grad, J.value
+
+    def turbulence_quantities(self):
+        """The turbdata.out row of calcTurbulenceQuantities (11 values)."""
+        out = np.zeros(11)
+        check(lib().cs3d_turbulence_quantities(self.h, _dptr(out)))
+        return out
+
+    def shear_layer_info(self):
+        """(17, Ny) per-plane statistics of shearLayerInfoCalc (rows as in cs3d.h)."""
+        out = np.zeros((17, self.cfg.Ny))
+        check(lib().cs3d_shear_layer_info(self.h, _dptr(out)))
+        return out
 
     def line_op(self, kind, direction, in_ptr, out_ptr):
         """kind 1/2/3 = deriv1/deriv2/filter on device arrays in the direction's

@@ -337,6 +337,7 @@ struct cs3d_handle {
     cudaEvent_t k_ev0 = nullptr;
     double *prim_out = nullptr;  // 7 FP64 fields for cs3d_get_field of primitives
     double *red = nullptr;       // reduction scratch
+    double *shear_buf = nullptr; // 17 x Ny per-plane statistics
     std::vector<void *> allocs;
     // discrete adjoint: workspace (allocated on first use) and the record of
     // the forward steps (checkpoints every adj_every steps)
@@ -1194,6 +1195,91 @@ extern "C" int cs3d_tgv_quantities(cs3d_handle *h, double out[7]) {
     out[4] = s[1];
     out[5] = s[5];
     out[6] = std::sqrt(s[4]);
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// calcTurbulenceQuantities and shearLayerInfoCalc
+// ---------------------------------------------------------------------
+template <typename T>
+static DiagArgs<T> diag_args(cs3d_handle *h) {
+    DiagArgs<T> a{};
+    a.g = h->g;
+    a.gas = h->gas;
+    a.q = h->q1;
+    for (int f = 0; f < 3; f++) {
+        a.dx[f] = (const T *)h->dx4[f];
+        a.dy[f] = (const T *)h->dy4[f];
+        a.dz[f] = (const T *)h->diag[f];
+    }
+    a.out = h->red;
+    return a;
+}
+
+template <typename T>
+static int turb_sums(cs3d_handle *h, int blocks, int pass, double meanRho, double *sums) {
+    DiagArgs<T> a = diag_args<T>(h);
+    a.meanRho = meanRho;
+    CS3D_CUDA(launch_turb<T>(a, blocks, pass, h->stream));
+    h->launches++;
+    std::vector<double> part((size_t)blocks * kTurbSums);
+    CS3D_CUDA(cudaMemcpyAsync(part.data(), h->red, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < kTurbSums; i++) sums[i] = 0.0;
+    for (int b = 0; b < blocks; b++)
+        for (int i = 0; i < kTurbSums; i++) sums[i] += part[(size_t)b * kTurbSums + i];
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_turbulence_quantities(cs3d_handle *h, double out[11]) {
+    if (!h || !out) return fail(CS3D_ERR_ARG, "null argument");
+    if (!h->store_diag || h->timeStep < 1)
+        return fail(CS3D_ERR_STATE, "run a step with CS3D_OPT_STORE_DIAGNOSTICS on first");
+    DeviceGuard dg(h->dev);
+    const int blocks = 512;  // 512 x 11 partial sums fit the reduction scratch
+    double s[kTurbSums], r2[kTurbSums], t[2];
+    int rc = h->mixed ? turb_sums<float>(h, blocks, 0, 0.0, s) : turb_sums<double>(h, blocks, 0, 0.0, s);
+    if (rc) return rc;
+    const double meanRho = s[0];
+    rc = h->mixed ? turb_sums<float>(h, blocks, 1, meanRho, r2) : turb_sums<double>(h, blocks, 1, meanRho, r2);
+    if (rc) return rc;
+    CS3D_CUDA(cudaMemcpyAsync(t, h->scal, 2 * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    // the derived quantities of CSolver_AWS.cpp:2119-2147, in its order
+    const double rhoprime = std::sqrt(r2[0]), dilprime = std::sqrt(s[9]), vortprime = std::sqrt(s[10]);
+    const double meanNu = s[1] / meanRho;
+    const double meanTurbDiss = s[2] / meanRho;
+    const double uprime = std::sqrt(s[3]), uiprime = std::sqrt(s[4]), urms = std::sqrt(s[5]);
+    const double turbMach = urms / s[6];
+    const double taylorMicro2 = uprime / uiprime;
+    const double taylorReyn3 = uprime * taylorMicro2 / meanNu;
+    const double pi = 3.14159265358979323846;
+    const double tau = std::sqrt(2.0 * pi) / 8.0 / uprime;
+    const double kolNu = std::pow(std::pow(meanNu, 3.0) / meanTurbDiss, 0.25);
+    const double row[11] = {t[1], tau, taylorReyn3, turbMach, meanTurbDiss, uprime, kolNu,
+                            rhoprime, dilprime, vortprime, s[8]};
+    for (int i = 0; i < 11; i++) out[i] = row[i];
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_shear_layer_info(cs3d_handle *h, double *out) {
+    if (!h || !out) return fail(CS3D_ERR_ARG, "null argument");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    DeviceGuard dg(h->dev);
+    const size_t n = 17 * (size_t)h->g.Ny;
+    if (!h->shear_buf) {
+        int rc = dalloc(h, (void **)&h->shear_buf, n * 8);
+        if (rc) return rc;
+    }
+    DiagArgs<double> a{};
+    a.g = h->g;
+    a.gas = h->gas;
+    a.q = h->q1;
+    a.out = h->shear_buf;
+    CS3D_CUDA(launch_shear_info(a, h->stream));
+    h->launches++;
+    CS3D_CUDA(cudaMemcpyAsync(out, h->shear_buf, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }
 

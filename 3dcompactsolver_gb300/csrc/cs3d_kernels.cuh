@@ -165,6 +165,21 @@ cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s);
 cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_tgv(const TgvArgs<T> &a, int blocks, cudaStream_t s);
+// calcTurbulenceQuantities / shearLayerInfoCalc sums over q1 and the
+// derivative fields of the last stage
+template <typename T>
+struct DiagArgs {
+    Geom g;
+    GasParams gas;
+    Q5 q;
+    const T *dx[3], *dy[3], *dz[3];
+    double *out;
+    double meanRho;
+};
+constexpr int kTurbSums = 11;
+template <typename T>
+cudaError_t launch_turb(const DiagArgs<T> &a, int blocks, int pass, cudaStream_t s);
+cudaError_t launch_shear_info(const DiagArgs<double> &a, cudaStream_t s);
 // allocation-free kinetic energy: kKeBlocks partials + the sum in a static
 // device array whose address ke_scratch_address returns
 constexpr int kKeBlocks = 1024;

@@ -384,6 +384,152 @@ cudaError_t launch_shadow(const ShadowArgs &a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------
+// calcTurbulenceQuantities (CSolver_AWS.cpp:2033-2173): per-block partial
+// sums, each term divided by the point count as the reference does; pass 0
+// gives meanRho, meanMu, meanTurbDiss, uprime, uiprime, urms, meanSOS,
+// taylor2_denom, meanKineticEng and the dilatation and vorticity sums, pass 1
+// the density variance about meanRho.
+// ---------------------------------------------------------------------
+template <int NS>
+__device__ __forceinline__ void block_sums(double (&s)[NS], double *out) {
+    __shared__ double red[NS][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        double v = s[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[i][wid] = v;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < NS) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+        out[threadIdx.x] = v;
+    }
+}
+
+template <typename T>
+__global__ void k_turb(DiagArgs<T> a, int pass) {
+    const double n = (double)a.g.npts;
+    double s[kTurbSums];
+#pragma unroll
+    for (int i = 0; i < kTurbSums; ++i) s[i] = 0.0;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        const double r = a.q.f[0][gi];
+        if (pass == 1) {
+            s[0] += ((r - a.meanRho) * (r - a.meanRho)) / n;
+            continue;
+        }
+        const double Ux = to_f64(a.dx[0][gi]), Vx = to_f64(a.dx[1][gi]), Wx = to_f64(a.dx[2][gi]);
+        const double Uy = to_f64(a.dy[0][gi]), Vy = to_f64(a.dy[1][gi]), Wy = to_f64(a.dy[2][gi]);
+        const double Uz = to_f64(a.dz[0][gi]), Vz = to_f64(a.dz[1][gi]), Wz = to_f64(a.dz[2][gi]);
+        const double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+        const double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
+        const double mu = a.gas.mu_ref * pow(p / (r * a.gas.R), 0.76);
+        const double sos = sqrt(a.gas.gamma * p / r);
+        const double dv = Ux + Vy + Wz;
+        const double S00 = 0.5 * (Ux + Ux) - (1.0 / 3.0) * dv, S11 = 0.5 * (Vy + Vy) - (1.0 / 3.0) * dv,
+                     S22 = 0.5 * (Wz + Wz) - (1.0 / 3.0) * dv;
+        const double S01 = 0.5 * (Uy + Vx), S02 = 0.5 * (Uz + Wx), S12 = 0.5 * (Vz + Wy);
+        double td = S00 * Ux;
+        td += S01 * Uy;
+        td += S02 * Uz;
+        td += S01 * Vx;
+        td += S11 * Vy;
+        td += S12 * Vz;
+        td += S02 * Wx;
+        td += S12 * Wy;
+        td += S22 * Wz;
+        td *= 2 * mu;
+        const double uvar = (U * U + V * V + W * W);
+        s[0] += r / n;
+        s[1] += mu / n;
+        s[2] += td / n;
+        s[3] += uvar / 3.0 / n;
+        s[4] += (Ux * Ux + Vy * Vy + Wz * Wz) / 3.0 / n;
+        s[5] += uvar / n;
+        s[6] += sos / n;
+        s[7] += (Ux * Ux) / n;
+        s[8] += r * uvar / n / 2.0;
+        s[9] += (dv * dv) / n;
+        const double wx = Wy - Vz, wy = Uz - Wx, wz = Vx - Uy;
+        s[10] += ((wx * wx + wy * wy + wz * wz)) / n;
+    }
+    block_sums<kTurbSums>(s, a.out + (size_t)blockIdx.x * kTurbSums);
+}
+
+template <typename T>
+cudaError_t launch_turb(const DiagArgs<T> &a, int blocks, int pass, cudaStream_t s) {
+    k_turb<T><<<blocks, 256, 0, s>>>(a, pass);
+    return cudaGetLastError();
+}
+template cudaError_t launch_turb<double>(const DiagArgs<double> &, int, int, cudaStream_t);
+template cudaError_t launch_turb<float>(const DiagArgs<float> &, int, int, cudaStream_t);
+
+// ---------------------------------------------------------------------
+// shearLayerInfoCalc (CSolver_AWS.cpp:2259-2456): one block per y plane; the
+// x-z means of rho, U, V, W, p, T, then the second moments about them.  The
+// reference adds the v'w' sum into uwprime (:2318) and leaves vwprime at 0;
+// rows 13 and 14 reproduce that, rows 15 and 16 hold u'w' and v'w'.
+// ---------------------------------------------------------------------
+__global__ void k_shear_info(DiagArgs<double> a) {
+    const int j = blockIdx.x;
+    const int Nx = a.g.Nx, Ny = a.g.Ny, Nz = a.g.Nz;
+    const long long nxz = (long long)Nx * Nz;
+    const double n = (double)nxz;
+    __shared__ double mean[6];
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    auto prims = [&](long long m, double v[6]) {
+        const int i = (int)(m % Nx), k = (int)(m / Nx);
+        const long long gi = ((long long)k * Ny + j) * Nx + i;
+        const double r = a.q.f[0][gi];
+        const double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+        const double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
+        v[0] = r; v[1] = U; v[2] = V; v[3] = W; v[4] = p; v[5] = p / (r * a.gas.R);
+    };
+    for (long long m = threadIdx.x; m < nxz; m += blockDim.x) {
+        double v[6];
+        prims(m, v);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) s[f] += v[f] / n;
+    }
+    double red6[6];
+    block_sums<6>(s, red6);  // threads 0..5 hold the plane sums
+    __syncthreads();
+    if (threadIdx.x < 6) mean[threadIdx.x] = red6[threadIdx.x];
+    __syncthreads();
+    double t[11];
+#pragma unroll
+    for (int f = 0; f < 11; ++f) t[f] = 0.0;
+    for (long long m = threadIdx.x; m < nxz; m += blockDim.x) {
+        double v[6], d[6];
+        prims(m, v);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            d[f] = v[f] - mean[f];
+            t[f] += d[f] * d[f] / n;
+        }
+        t[6] += d[1] * d[2] / n;
+        t[7] += d[1] * d[3] / n;
+        t[7] += d[2] * d[3] / n;
+        t[9] += d[1] * d[3] / n;
+        t[10] += d[2] * d[3] / n;
+    }
+    double red11[11];
+    __syncthreads();
+    block_sums<11>(t, red11);
+    if (threadIdx.x < 6) a.out[(size_t)threadIdx.x * Ny + j] = mean[threadIdx.x];
+    if (threadIdx.x < 11) a.out[(size_t)(6 + threadIdx.x) * Ny + j] = red11[threadIdx.x];
+}
+
+cudaError_t launch_shear_info(const DiagArgs<double> &a, cudaStream_t s) {
+    k_shear_info<<<a.g.Ny, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
 // Kinetic energy without any allocation: the KEsum column of the
 // Taylor-Green diagnostics (CSolver_AWS.cpp:2175-2236) from four device
 // arrays, with its partial sums in a fixed file-scope scratch array instead

@@ -200,6 +200,24 @@ int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
  * requires CS3D_OPT_STORE_DIAGNOSTICS to have been on during that stage. */
 int cs3d_tgv_quantities(cs3d_handle *h, double out[7]);
 
+/* calcTurbulenceQuantities (CSolver_AWS.cpp:2033-2173): out[0..10] = the
+ * turbdata.out row -- time, tau, taylorReyn3, turbMach, meanTurbDiss, uprime,
+ * kolNu, rhoprime, dilprime, vortprime, meanKineticEng.  Derivatives of the
+ * last stage as in the reference; requires CS3D_OPT_STORE_DIAGNOSTICS. */
+int cs3d_turbulence_quantities(cs3d_handle *h, double out[11]);
+
+/* shearLayerInfoCalc (CSolver_AWS.cpp:2259-2456): per y plane j, x-z means
+ * and second moments of rho, U, V, W, p, T of the current state; out holds
+ * 17*Ny doubles, out[k*Ny + j] with k = 0 rhoAvg, 1 uAvg, 2 vAvg, 3 wAvg,
+ * 4 pAvg, 5 tAvg, 6 rhoprime2, 7 uprime2, 8 vprime2, 9 wprime2, 10 pprime2,
+ * 11 tprime2, 12 uvprime, 13 uwprime and 14 vwprime as the reference writes
+ * them (it adds the v'w' sum into uwprime and leaves vwprime 0, :2317-2318),
+ * 15 u'w' and 16 v'w' each on its own.  The reference evaluates it in
+ * postStep before the sponge update: call it between the last cs3d_sub_step
+ * and cs3d_post_step to see the same state; it runs on every call (the
+ * reference only on steps that are multiples of 25). */
+int cs3d_shear_layer_info(cs3d_handle *h, double *out);
+
 /* ---- discrete adjoint of the time steps --------------------------------
  * No counterpart in the reference.  Gradient of an objective J of the state
  * after n steps with respect to the state before them, by the transposed

@@ -1067,6 +1067,130 @@ void or_tgv_quantities(or_solver *s, double out[7]) {
     out[6] = sqrt(dil);
 }
 
+/* calcTurbulenceQuantities (CSolver_AWS.cpp:2033-2173): the row of
+ * turbdata.out -- time, tau, taylorReyn3, turbMach, meanTurbDiss, uprime,
+ * kolNu, rhoprime, dilprime, vortprime, meanKineticEng -- over the derivative
+ * fields of the last stage and the primitives of q1. */
+void or_turbulence_quantities(or_solver *s, double out[11]) {
+    double **A = s->a;
+    const double Ntot = (double)(s->Nx * s->Ny * s->Nz);
+    double meanRho = 0, meanMu = 0, meanTurbDiss = 0, uprime = 0, uiprime = 0, urms = 0, meanSOS = 0,
+           taylor2_denom = 0, meanKineticEng = 0;
+#pragma omp parallel for reduction(+ : meanRho, meanMu, meanTurbDiss, uprime, uiprime, urms, meanSOS, \
+                                   taylor2_denom, meanKineticEng) schedule(static)
+    for (long ip = 0; ip < (long)s->N; ip++) {
+        double Ux = A[A_UX][ip], Uy = A[A_UY][ip], Uz = A[A_UZ][ip];
+        double Vx = A[A_VX][ip], Vy = A[A_VY][ip], Vz = A[A_VZ][ip];
+        double Wx = A[A_WX][ip], Wy = A[A_WY][ip], Wz = A[A_WZ][ip];
+        double S[3][3];
+        S[0][0] = 0.5 * (Ux + Ux) - (1.0 / 3.0) * (Ux + Vy + Wz);
+        S[1][1] = 0.5 * (Vy + Vy) - (1.0 / 3.0) * (Ux + Vy + Wz);
+        S[2][2] = 0.5 * (Wz + Wz) - (1.0 / 3.0) * (Ux + Vy + Wz);
+        S[0][1] = S[1][0] = 0.5 * (Uy + Vx);
+        S[0][2] = S[2][0] = 0.5 * (Uz + Wx);
+        S[1][2] = S[2][1] = 0.5 * (Vz + Wy);
+        double td = S[0][0] * Ux;
+        td += S[0][1] * Uy;
+        td += S[0][2] * Uz;
+        td += S[1][0] * Vx;
+        td += S[1][1] * Vy;
+        td += S[1][2] * Vz;
+        td += S[2][0] * Wx;
+        td += S[2][1] * Wy;
+        td += S[2][2] * Wz;
+        td *= 2 * A[A_MU][ip];
+        double U = A[A_U][ip], V = A[A_V][ip], W = A[A_W][ip];
+        double up2 = (U * U + V * V + W * W) / 3.0;
+        double uvar = (U * U + V * V + W * W);
+        double uip2 = (Ux * Ux + Vy * Vy + Wz * Wz) / 3.0;
+        double ke = A[A_RHO1][ip] * uvar;
+        meanRho += A[A_RHO1][ip] / Ntot;
+        meanMu += A[A_MU][ip] / Ntot;
+        meanTurbDiss += td / Ntot;
+        uprime += up2 / Ntot;
+        uiprime += uip2 / Ntot;
+        urms += uvar / Ntot;
+        meanSOS += A[A_SOS][ip] / Ntot;
+        taylor2_denom += (Ux * Ux) / Ntot;
+        meanKineticEng += ke / Ntot / 2.0;
+    }
+    double rhoprime = 0, dilprime = 0, vortprime = 0;
+#pragma omp parallel for reduction(+ : rhoprime, dilprime, vortprime) schedule(static)
+    for (long ip = 0; ip < (long)s->N; ip++) {
+        double r = A[A_RHO1][ip];
+        double Ux = A[A_UX][ip], Uy = A[A_UY][ip], Uz = A[A_UZ][ip];
+        double Vx = A[A_VX][ip], Vy = A[A_VY][ip], Vz = A[A_VZ][ip];
+        double Wx = A[A_WX][ip], Wy = A[A_WY][ip], Wz = A[A_WZ][ip];
+        rhoprime += ((r - meanRho) * (r - meanRho)) / Ntot;
+        dilprime += ((Ux + Vy + Wz) * (Ux + Vy + Wz)) / Ntot;
+        double wx = Wy - Vz, wy = Uz - Wx, wz = Vx - Uy;
+        vortprime += ((wx * wx + wy * wy + wz * wz)) / Ntot;
+    }
+    (void)taylor2_denom;
+    rhoprime = sqrt(rhoprime);
+    dilprime = sqrt(dilprime);
+    vortprime = sqrt(vortprime);
+    double meanNu = meanMu / meanRho;
+    meanTurbDiss /= meanRho;
+    uprime = sqrt(uprime);
+    uiprime = sqrt(uiprime);
+    urms = sqrt(urms);
+    double turbMach = urms / meanSOS;
+    double taylorMicro2 = uprime / uiprime;
+    double taylorReyn3 = uprime * taylorMicro2 / meanNu;
+    double k0 = 8.0;
+    const double pi = 3.14159265358979323846; /* M_PI of the reference's <cmath> */
+    double tau = sqrt(2.0 * pi) / k0 / uprime;
+    double kolNu = pow(pow(meanNu, 3.0) / meanTurbDiss, 0.25);
+    out[0] = s->time;
+    out[1] = tau;
+    out[2] = taylorReyn3;
+    out[3] = turbMach;
+    out[4] = meanTurbDiss;
+    out[5] = uprime;
+    out[6] = kolNu;
+    out[7] = rhoprime;
+    out[8] = dilprime;
+    out[9] = vortprime;
+    out[10] = meanKineticEng;
+}
+
+/* shearLayerInfoCalc (CSolver_AWS.cpp:2259-2456): per y plane, the x-z means
+ * and second moments of rho, U, V, W, p, T of q1.  out[k*Ny + j] with k =
+ * 0 rhoAvg, 1 uAvg, 2 vAvg, 3 wAvg, 4 pAvg, 5 tAvg, 6 rhoprime2, 7 uprime2,
+ * 8 vprime2, 9 wprime2, 10 pprime2, 11 tprime2, 12 uvprime, 13 uwprime as the
+ * reference writes it (the u'w' and v'w' sums both, :2317-2318), 14 vwprime
+ * as the reference writes it (0), 15 u'w' and 16 v'w' each on its own. */
+void or_shear_layer_info(or_solver *s, double *out) {
+    double **A = s->a;
+    const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
+    const double nxz = (double)(Nx * Nz);
+    double *o = out;
+    for (long m = 0; m < 17L * Ny; m++) o[m] = 0.0;
+    const double *F[6] = {A[A_RHO1], A[A_U], A[A_V], A[A_W], A[A_P], A[A_T]};
+    for (int k = 0; k < Nz; k++)
+        for (int j = 0; j < Ny; j++)
+            for (int i = 0; i < Nx; i++) {
+                size_t ii = IDX(i, j, k);
+                for (int f = 0; f < 6; f++) o[f * Ny + j] += F[f][ii] / nxz;
+            }
+    for (int k = 0; k < Nz; k++)
+        for (int j = 0; j < Ny; j++)
+            for (int i = 0; i < Nx; i++) {
+                size_t ii = IDX(i, j, k);
+                double d[6];
+                for (int f = 0; f < 6; f++) {
+                    d[f] = F[f][ii] - o[f * Ny + j];
+                    o[(6 + f) * Ny + j] += d[f] * d[f] / nxz;
+                }
+                o[12 * Ny + j] += d[1] * d[2] / nxz;
+                o[13 * Ny + j] += d[1] * d[3] / nxz;
+                o[13 * Ny + j] += d[2] * d[3] / nxz;
+                o[15 * Ny + j] += d[1] * d[3] / nxz;
+                o[16 * Ny + j] += d[2] * d[3] / nxz;
+            }
+}
+
 /* Single operator on contiguous lines: kind 1/2/3 as line_apply, nlines
  * lines of length N with spacing dh. */
 void or_line_op(int kind, int bc_type, int N, double dh, double alphaF, long nlines, const double *in,

@@ -74,6 +74,8 @@ def port_lib(flavour="strict"):
         lib.or_set_named.argtypes = [_VP, ctypes.c_char_p, _DP]
         lib.or_get_scalars.argtypes = [_VP, _DP, _DP, ctypes.POINTER(ctypes.c_int)]
         lib.or_tgv_quantities.argtypes = [_VP, _DP]
+        lib.or_turbulence_quantities.argtypes = [_VP, _DP]
+        lib.or_shear_layer_info.argtypes = [_VP, _DP]
         lib.or_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_long, _DP, _DP]
         lib.or_num_threads.restype = ctypes.c_int
@@ -102,6 +104,8 @@ def ref_lib(flavour="strict"):
         lib.ref_get_named.argtypes = [_VP, ctypes.c_char_p, _DP]
         lib.ref_get_scalars.argtypes = [_VP, _DP, _DP, ctypes.POINTER(ctypes.c_int)]
         lib.ref_destroy.argtypes = [_VP]
+        lib.ref_turbulence_quantities.argtypes = [_VP]
+        lib.ref_shear_layer_info.argtypes = [_VP]
         lib.ref_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, _DP, _DP]
@@ -184,6 +188,18 @@ class OraclePort(_Base):
         self.lib.or_tgv_quantities(self.h, _ptr(out))
         return out
 
+    def turbulence_quantities(self):
+        """The turbdata.out row of calcTurbulenceQuantities (11 values)."""
+        out = np.zeros(11)
+        self.lib.or_turbulence_quantities(self.h, _ptr(out))
+        return out
+
+    def shear_layer_info(self):
+        """(17, Ny) per-plane statistics of shearLayerInfoCalc (see the C source)."""
+        out = np.zeros((17, self.cfg.Ny))
+        self.lib.or_shear_layer_info(self.h, _ptr(out))
+        return out
+
 
 class RefSolver(_Base):
     """The reference's own CSolver_AWS + RK4/TVDRK3 (oracle/_ref)."""
@@ -228,6 +244,35 @@ class RefSolver(_Base):
         dt, t, ts = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
         self.lib.ref_get_scalars(self.h, ctypes.byref(dt), ctypes.byref(t), ctypes.byref(ts))
         return dt.value, t.value, ts.value
+
+    def _in_tmpdir(self, fn):
+        import tempfile
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                fn()
+                return {f: open(os.path.join(d, f)).read() for f in os.listdir(d)}
+            finally:
+                os.chdir(cwd)
+
+    def turbulence_quantities(self):
+        """The reference's calcTurbulenceQuantities: its turbdata.out row."""
+        files = self._in_tmpdir(lambda: self.lib.ref_turbulence_quantities(self.h))
+        return np.array([float(x) for x in files["turbdata.out"].split()])
+
+    def shear_layer_info(self):
+        """The reference's shearLayerInfoCalc, read back from its .out files, in
+        the row order of the restatement (rows 2, 3, 4, 5, 15, 16 are not
+        written by the reference and come back as NaN)."""
+        files = self._in_tmpdir(lambda: self.lib.ref_shear_layer_info(self.h))
+        names = {0: "rhoAvg", 1: "uAvg", 6: "rhoprime2", 7: "uprime2", 8: "vprime2", 9: "wprime2",
+                 10: "pprime2", 11: "tprime2", 12: "uvprime", 13: "uwprime", 14: "vwprime"}
+        out = np.full((17, self.cfg.Ny), np.nan)
+        for k, nm in names.items():
+            vals = [float(x) for x in files[nm + ".out"].split()]
+            out[k] = vals[1:]  # the first value is the time
+        return out
 
 
 def line_op_port(kind, bc_type, N, dh, alphaF, lines, flavour="strict"):

@@ -189,6 +189,22 @@ int ref_get_named(void *hp, const char *name, double *out) {
     return 1;
 }
 
+// The reference's own diagnostics; they write their rows to files in the
+// current directory (turbdata.out, rhoprime2.out, ...).  shearLayerInfoCalc
+// runs only on steps that are multiples of 25 (CSolver_AWS.cpp:2265), so the
+// step counter is set to 0 around the call.
+void ref_turbulence_quantities(void *hp) {
+    RefHandle *h = (RefHandle *)hp;
+    h->cs->calcTurbulenceQuantities();
+}
+void ref_shear_layer_info(void *hp) {
+    RefHandle *h = (RefHandle *)hp;
+    int ts = h->cs->timeStep;
+    h->cs->timeStep = 0;
+    h->cs->shearLayerInfoCalc();
+    h->cs->timeStep = ts;
+}
+
 void ref_get_scalars(void *hp, double *dt, double *time, int *time_step) {
     RefHandle *h = (RefHandle *)hp;
     *dt = h->ts->dt;

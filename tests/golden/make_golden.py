@@ -7,6 +7,8 @@ and the reference harness built by `make -C oracle ref`.  Writes:
   taylorgreen_run128_head.txt  rows 1-3 of taylorgreen_vortex/taylorgreen_run128/taylorgreen.out
   ref_<case>.npz               q1 after 3 steps of the reference's own CSolver_AWS + RK4/TVDRK3
                                (oracle/_ref, strict build), with dt, time and timeStep
+  ref_diagnostics.npz          the reference's calcTurbulenceQuantities row and shearLayerInfoCalc
+                               profiles after 2 steps + the stages of a third (before postStep's sponge)
   ref_lineops.npz              the reference's calc1stDerivField / calc2ndDerivField /
                                filterField on seeded random fields
 
@@ -37,6 +39,8 @@ CASES = {
     "shear": lambda: cases.shear_layer(16, 12, 10, precision=_abi.FP64),
 }
 NSTEPS = 3
+DIAG_EXTRA = {"hit12": lambda: cases.hit(12, seed=3, k0=3.0)}
+DIAG_CASES = ["tgv12", "hit12", "shear", "wall_moving_sponge"]
 
 # single operators: (kind, dir, bc_type, (Nx, Ny, Nz))
 LINEOPS = [(k, d, bc, n) for k in (1, 2, 3) for d in (0, 1, 2) for bc in (0, 1)
@@ -60,6 +64,22 @@ def main():
         dt, t, ts = r.scalars()
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), q1=r.conserved(), dt=dt, time=t,
                             timeStep=ts, nsteps=NSTEPS)
+    # the reference's calcTurbulenceQuantities and shearLayerInfoCalc after two
+    # steps and the stages of a third, before its post-step (the order of
+    # CSolver_AWS::postStep, CSolver_AWS.cpp:2930-2938)
+    diag = {}
+    for name in DIAG_CASES:
+        cfg, ic = CASES[name]() if name in CASES else DIAG_EXTRA[name]()
+        r = oracle.RefSolver(cfg)
+        r.set_initial_conditions(*ic)
+        r.run(2)
+        r.pre_step()
+        nst = 3 if cfg.rk == _abi.TVDRK3 else 4
+        for st in range(1, nst + 1):
+            r.sub_step(st, st == nst)
+        diag[f"{name}_turb"] = r.turbulence_quantities()
+        diag[f"{name}_shear"] = r.shear_layer_info()
+    np.savez_compressed(os.path.join(HERE, "ref_diagnostics.npz"), **diag)
     rng = np.random.default_rng(2024)
     out = {}
     for idx, (kind, d, bc, n) in enumerate(LINEOPS):

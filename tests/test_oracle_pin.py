@@ -98,3 +98,63 @@ def test_port_bit_identical_to_live_reference(oracle, cases, name):
         r.step()
     for nm in ("rho1", "rhoU1", "rhoV1", "rhoW1", "rhoE1", "U", "T", "mu", "Ux", "Wyz", "Tzz"):
         assert np.array_equal(p.get(nm), r.get(nm)), nm
+
+
+DIAG_CASES = ["tgv12", "hit12", "shear", "wall_moving_sponge"]
+
+
+def _diag_case(cases, name):
+    if name == "hit12":
+        return cases.hit(12, seed=3, k0=3.0)
+    return _case(cases, name)
+
+
+def diag_compare(turb, info, g, name, tol):
+    """turbdata row and shear-layer profiles against the reference's (rows the
+    reference does not write are NaN in the fixture)."""
+    ref = g[f"{name}_turb"]
+    for i, (a, b) in enumerate(zip(turb, ref)):
+        assert abs(a - b) <= tol * abs(b) + 1e-300, (name, "turb", i, a, b)
+    ref = g[f"{name}_shear"]
+    vvar = np.nanmax(np.abs(ref[7:10]))
+    for k in range(ref.shape[0]):
+        if np.isnan(ref[k]).all():
+            continue
+        # velocity means against the velocity scale and velocity (co)variances
+        # against the largest variance: for the Taylor-Green vortex the plane
+        # means and the covariances are rounding noise about zero
+        nat = np.sqrt(vvar) if 1 <= k <= 3 else (vvar if 7 <= k <= 9 or k >= 12 else 0.0)
+        scale = max(np.abs(ref[k]).max(), nat, 1e-300)
+        # a variance about a mean m picks up 2 sqrt(var) * (state rounding, ~1e-13 m)
+        atol = 0.0
+        if 6 <= k <= 11 and not np.isnan(ref[k - 6]).all():
+            atol = 2.0 * np.sqrt(np.abs(ref[k]).max()) * 1e-13 * np.abs(ref[k - 6]).max()
+        assert np.abs(info[k] - ref[k]).max() <= tol * scale + atol, (name, "shear", k)
+
+
+def _stages_then(sv, cfg):
+    import importlib
+    _abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    nst = 3 if cfg.rk == _abi.TVDRK3 else 4
+    sv.run(2)
+    sv.pre_step()
+    for st in range(1, nst + 1):
+        sv.sub_step(st, st == nst)
+
+
+@pytest.mark.parametrize("name", DIAG_CASES)
+def test_port_diagnostics_match_reference(oracle, cases, name):
+    """calcTurbulenceQuantities and shearLayerInfoCalc: the restatement against
+    the reference's own output files (tests/golden/ref_diagnostics.npz); sums in
+    another order, so not bit for bit."""
+    g = load_golden("ref_diagnostics.npz")
+    cfg, ic = _diag_case(cases, name)
+    p = oracle.OraclePort(cfg)
+    p.set_initial_conditions(*ic)
+    _stages_then(p, cfg)
+    info = p.shear_layer_info()
+    # the reference writes uwprime = u'w' + v'w' and vwprime = 0 (CSolver_AWS.cpp:2317-2318)
+    sc = np.abs(info[7:10]).max()  # covariances are measured against the velocity variances
+    assert np.abs(info[13] - (info[15] + info[16])).max() <= 1e-12 * sc
+    assert not info[14].any()
+    diag_compare(p.turbulence_quantities(), info, g, name, 1e-11)
