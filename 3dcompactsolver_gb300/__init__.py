@@ -75,6 +75,8 @@ def lib():
             getattr(L, name).argtypes = [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.cs3d_tgv_quantities.argtypes = [_H, _DP]
         L.cs3d_turbulence_quantities.argtypes = [_H, _DP]
+        L.cs3d_dump_solution.argtypes = [_H, ctypes.c_char_p]
+        L.cs3d_load_solution.argtypes = [_H, ctypes.c_char_p, ctypes.c_int, ctypes.c_double]
         L.cs3d_shear_layer_info.argtypes = [_H, _DP]
         L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
                                         ctypes.c_int]
@@ -224,6 +226,14 @@ class Solver:
         sp = _dptr(keep) if keep is not None else None
         check(lib().cs3d_adjoint_backward(self.h, int(objective), sp, _dptr(grad), ctypes.byref(J)))
         return grad, J.value
+
+    def dump_solution(self, prefix=""):
+        """Write q1 in dumpSolution's format: <prefix>rho.out.<step> ... rhoE."""
+        check(lib().cs3d_dump_solution(self.h, prefix.encode()))
+
+    def load_solution(self, prefix, time_step, time):
+        """Restart from dumpSolution files of step time_step (the time is not in them)."""
+        check(lib().cs3d_load_solution(self.h, prefix.encode(), int(time_step), float(time)))
 
     def turbulence_quantities(self):
         """The turbdata.out row of calcTurbulenceQuantities (11 values)."""

@@ -7,7 +7,7 @@ import ctypes
 
 OK, ERR_ARG, ERR_SHAPE, ERR_CUDA, ERR_NAN, ERR_ALLOC, ERR_STATE, ERR_NODEV = range(8)
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_SHAPE", 3: "ERR_CUDA", 4: "ERR_NAN",
-                5: "ERR_ALLOC", 6: "ERR_STATE", 7: "ERR_NODEV"}
+                5: "ERR_ALLOC", 6: "ERR_STATE", 7: "ERR_NODEV", 8: "ERR_IO"}
 
 PERIODIC_SOLVE, DIRICHLET_SOLVE = 0, 1
 PERIODIC, SPONGE, ADIABATIC_WALL, MOVING_ADIABATIC_WALL, INLET = 0, 1, 2, 3, 4

@@ -678,6 +678,8 @@ static int launch_cfl_reduce(cs3d_handle *h) {
     return CS3D_OK;
 }
 
+static int init_after_state(cs3d_handle *h);
+
 extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, const double *p0, const double *U0,
                                            const double *V0, const double *W0) {
     if (!h || !rho0 || !p0 || !U0 || !V0 || !W0) return fail(CS3D_ERR_ARG, "null argument");
@@ -712,10 +714,20 @@ extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, c
         CS3D_CUDA(launch_ic_wall_eos(a, h->stream));
         h->launches++;
     }
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    CS3D_CUDA(cudaFree(tmp));
+    return init_after_state(h);
+}
+
+// Everything that follows a new state q1: sponge averages (SpongeBC starts
+// them at the state), the mixed filter's reference values (the state's field
+// means), the FP32 shadow, counters, dt/time, the NaN flag and the CFL
+// maximum for the first step.
+static int init_after_state(cs3d_handle *h) {
+    const size_t n = (size_t)h->g.npts;
     if (h->sponge)
         for (int f = 0; f < 5; f++)
             CS3D_CUDA(cudaMemcpyAsync(h->savg.f[f], h->q1.f[f], n * 8, cudaMemcpyDeviceToDevice, h->stream));
-    // reference values of the mixed filter: the field means of the initial state
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     if (h->mixed) {
         std::vector<double> hb(n);
@@ -726,7 +738,6 @@ extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, c
             h->fref[f] = (double)(s / (long double)n);
         }
     }
-    CS3D_CUDA(cudaFree(tmp));
     if (h->mixed) {
         int r = launch_shadow_of(h, h->q1, h->q1s);
         if (r) return r;
@@ -1812,6 +1823,64 @@ extern "C" int cs3d_rhs_vjp(cs3d_handle *h, const double *q_host, const double *
     const size_t n = (size_t)h->g.npts;
     for (int f = 0; f < 5; f++)
         CS3D_CUDA(cudaMemcpyAsync(out_host + (size_t)f * n, OUT[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// dumpSolution format (CSolver_AWS.cpp:2493-2535): q1 as five raw FP64
+// files in XYZ order, no header, named rho.out.<step> ... rhoE.out.<step>
+// ---------------------------------------------------------------------
+static const char *const kDumpNames[5] = {"rho", "rhoU", "rhoV", "rhoW", "rhoE"};
+
+static std::string dump_path(const char *prefix, int f, int step) {
+    return std::string(prefix ? prefix : "") + kDumpNames[f] + ".out." + std::to_string(step);
+}
+
+extern "C" int cs3d_dump_solution(cs3d_handle *h, const char *prefix) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    std::vector<double> buf(n);
+    for (int f = 0; f < 5; f++) {
+        CS3D_CUDA(cudaMemcpyAsync(buf.data(), h->q1.f[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
+        CS3D_CUDA(cudaStreamSynchronize(h->stream));
+        const std::string path = dump_path(prefix, f, h->timeStep);
+        FILE *fp = fopen(path.c_str(), "wb");
+        if (!fp) return fail(CS3D_ERR_IO, "cannot open %s for writing", path.c_str());
+        const size_t w = fwrite(buf.data(), sizeof(double), n, fp);
+        const int c = fclose(fp);
+        if (w != n || c != 0) return fail(CS3D_ERR_IO, "short write to %s", path.c_str());
+    }
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_load_solution(cs3d_handle *h, const char *prefix, int time_step, double time) {
+    if (!h) return fail(CS3D_ERR_ARG, "null handle");
+    if (time_step < 0) return fail(CS3D_ERR_ARG, "time_step = %d", time_step);
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    std::vector<double> buf(n);
+    for (int f = 0; f < 5; f++) {
+        const std::string path = dump_path(prefix, f, time_step);
+        FILE *fp = fopen(path.c_str(), "rb");
+        if (!fp) return fail(CS3D_ERR_IO, "cannot open %s", path.c_str());
+        const size_t r = fread(buf.data(), sizeof(double), n, fp);
+        const int extra = fgetc(fp);
+        fclose(fp);
+        if (r != n || extra != EOF)
+            return fail(CS3D_ERR_SHAPE, "%s does not hold %zu doubles (%d x %d x %d)", path.c_str(), n, h->g.Nx,
+                        h->g.Ny, h->g.Nz);
+        CS3D_CUDA(cudaMemcpyAsync(h->q1.f[f], buf.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
+        CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    int rc = init_after_state(h);
+    if (rc) return rc;
+    h->timeStep = time_step;
+    h->filterTimeStep = time_step / h->cfg.filter_step;  // filtered steps so far
+    double sc[2] = {0.0, time};
+    CS3D_CUDA(cudaMemcpyAsync(h->scal, sc, 2 * 8, cudaMemcpyHostToDevice, h->stream));
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }

@@ -30,6 +30,7 @@ extern "C" {
 #define CS3D_ERR_ALLOC   5  /* device or host allocation failed             */
 #define CS3D_ERR_STATE   6  /* call made in the wrong order                 */
 #define CS3D_ERR_NODEV   7  /* no CUDA device visible                       */
+#define CS3D_ERR_IO      8  /* a file could not be opened, read or written  */
 
 /* ---- enumerations (values equal the reference's enums) ---------------- */
 /* BC::BCType, BC.hpp:10 */
@@ -217,6 +218,21 @@ int cs3d_turbulence_quantities(cs3d_handle *h, double out[11]);
  * and cs3d_post_step to see the same state; it runs on every call (the
  * reference only on steps that are multiples of 25). */
 int cs3d_shear_layer_info(cs3d_handle *h, double *out);
+
+/* ---- restart files ------------------------------------------------------
+ * dumpSolution's format (CSolver_AWS.cpp:2493-2535): the conserved state q1
+ * as five raw FP64 files in XYZ order with no header, named
+ * <prefix>rho.out.<step>, rhoU, rhoV, rhoW, rhoE (prefix may be a directory
+ * ending in '/', or ""); <step> is the solver's step count.
+ * cs3d_load_solution reads such files (the reference's own or ours) into q1,
+ * sets the step count and the time (the format stores neither; pass the
+ * time the run had), and prepares the handle as cs3d_set_initial_conditions
+ * does.  In the FP64 form without SPONGE faces or bands the run then
+ * continues bit for bit as if it had not stopped; otherwise the sponge
+ * averages restart from the loaded state and the mixed form's filter
+ * reference values are the loaded state's field means. */
+int cs3d_dump_solution(cs3d_handle *h, const char *prefix);
+int cs3d_load_solution(cs3d_handle *h, const char *prefix, int time_step, double time);
 
 /* ---- discrete adjoint of the time steps --------------------------------
  * No counterpart in the reference.  Gradient of an objective J of the state

@@ -106,6 +106,7 @@ def ref_lib(flavour="strict"):
         lib.ref_destroy.argtypes = [_VP]
         lib.ref_turbulence_quantities.argtypes = [_VP]
         lib.ref_shear_layer_info.argtypes = [_VP]
+        lib.ref_dump_solution.argtypes = [_VP]
         lib.ref_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, _DP, _DP]
@@ -253,6 +254,18 @@ class RefSolver(_Base):
             try:
                 fn()
                 return {f: open(os.path.join(d, f)).read() for f in os.listdir(d)}
+            finally:
+                os.chdir(cwd)
+
+    def dump_solution(self):
+        """The reference's dumpSolution: {file name: bytes} of what it writes."""
+        import tempfile
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                self.lib.ref_dump_solution(self.h)
+                return {f: open(os.path.join(d, f), "rb").read() for f in os.listdir(d)}
             finally:
                 os.chdir(cwd)
 

@@ -205,6 +205,16 @@ void ref_shear_layer_info(void *hp) {
     h->cs->timeStep = ts;
 }
 
+// dumpSolution writes only on steps that are multiples of dumpStep
+// (CSolver_AWS.cpp:2497); dumpStep is set to 1 around the call.
+void ref_dump_solution(void *hp) {
+    RefHandle *h = (RefHandle *)hp;
+    int ds = h->ts->dumpStep;
+    h->ts->dumpStep = 1;
+    h->cs->dumpSolution();
+    h->ts->dumpStep = ds;
+}
+
 void ref_get_scalars(void *hp, double *dt, double *time, int *time_step) {
     RefHandle *h = (RefHandle *)hp;
     *dt = h->ts->dt;

@@ -158,3 +158,22 @@ def test_port_diagnostics_match_reference(oracle, cases, name):
     assert np.abs(info[13] - (info[15] + info[16])).max() <= 1e-12 * sc
     assert not info[14].any()
     diag_compare(p.turbulence_quantities(), info, g, name, 1e-11)
+
+
+def test_reference_dump_format(oracle, cases):
+    """dumpSolution's format, read from the reference itself: five raw FP64
+    files of q1 in XYZ order, no header, named <field>.out.<step>."""
+    if not oracle.ref_available():
+        pytest.skip("reference harness not built here")
+    cfg, ic = _case(cases, "wall")
+    r = oracle.RefSolver(cfg)
+    r.set_initial_conditions(*ic)
+    for _ in range(3):
+        r.step()
+    files = r.dump_solution()
+    names = ["rho", "rhoU", "rhoV", "rhoW", "rhoE"]
+    assert sorted(files) == sorted(f"{n}.out.3" for n in names)
+    for f, n in enumerate(names):
+        data = np.frombuffer(files[f"{n}.out.3"], dtype="<f8")
+        assert data.size == cfg.npts
+        assert np.array_equal(data, r.get(["rho1", "rhoU1", "rhoV1", "rhoW1", "rhoE1"][f]).reshape(-1))
