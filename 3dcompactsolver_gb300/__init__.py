@@ -76,6 +76,7 @@ def lib():
         L.cs3d_tgv_quantities.argtypes = [_H, _DP]
         L.cs3d_turbulence_quantities.argtypes = [_H, _DP]
         L.cs3d_dump_solution.argtypes = [_H, ctypes.c_char_p]
+        L.cs3d_aero_optics.argtypes = [_H, ctypes.c_int, ctypes.c_double, _DP]
         L.cs3d_load_solution.argtypes = [_H, ctypes.c_char_p, ctypes.c_int, ctypes.c_double]
         L.cs3d_shear_layer_info.argtypes = [_H, _DP]
         L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
@@ -226,6 +227,12 @@ class Solver:
         sp = _dptr(keep) if keep is not None else None
         check(lib().cs3d_adjoint_backward(self.h, int(objective), sp, _dptr(grad), ctypes.byref(J)))
         return grad, J.value
+
+    def aero_optics(self, num_angles=5, max_angle=70.0):
+        """Optical-path integrals of the density, shape (num_angles, Nz, Nx)."""
+        out = np.zeros((num_angles, self.cfg.Nz, self.cfg.Nx))
+        check(lib().cs3d_aero_optics(self.h, int(num_angles), float(max_angle), _dptr(out)))
+        return out
 
     def dump_solution(self, prefix=""):
         """Write q1 in dumpSolution's format: <prefix>rho.out.<step> ... rhoE."""

@@ -338,6 +338,8 @@ struct cs3d_handle {
     double *prim_out = nullptr;  // 7 FP64 fields for cs3d_get_field of primitives
     double *red = nullptr;       // reduction scratch
     double *shear_buf = nullptr; // 17 x Ny per-plane statistics
+    double *aero_buf = nullptr;  // optical path integrals
+    size_t aero_cap = 0;
     std::vector<void *> allocs;
     // discrete adjoint: workspace (allocated on first use) and the record of
     // the forward steps (checkpoints every adj_every steps)
@@ -1290,6 +1292,55 @@ extern "C" int cs3d_shear_layer_info(cs3d_handle *h, double *out) {
     CS3D_CUDA(launch_shear_info(a, h->stream));
     h->launches++;
     CS3D_CUDA(cudaMemcpyAsync(out, h->shear_buf, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// AeroOptics::computeAO with generateBaseBeamDiff (AeroOptics.cpp:3-93)
+// ---------------------------------------------------------------------
+extern "C" int cs3d_aero_optics(cs3d_handle *h, int num_angles, double max_angle, double *opl) {
+    if (!h || !opl) return fail(CS3D_ERR_ARG, "null argument");
+    if (num_angles < 2 || num_angles > kAeroMaxAngles)
+        return fail(CS3D_ERR_ARG, "num_angles = %d (2 .. %d)", num_angles, kAeroMaxAngles);
+    if (!(max_angle >= 0.0 && max_angle < 90.0)) return fail(CS3D_ERR_ARG, "max_angle = %g degrees", max_angle);
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)num_angles * h->g.Nx * h->g.Nz;
+    if (n > h->aero_cap) {
+        void *p = nullptr;
+        int rc = dalloc(h, &p, n * 8);
+        if (rc) return rc;
+        h->aero_buf = (double *)p;
+        h->aero_cap = n;
+    }
+    AeroArgs a{};
+    a.g = h->g;
+    a.rho = h->q1.f[0];
+    a.Lx = h->cfg.Lx; a.Ly = h->cfg.Ly; a.Lz = h->cfg.Lz;
+    a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
+    // AeroOptics.hpp:56-63 and generateBaseBeamDiff
+    a.lower = 0.2 * h->cfg.Ly;
+    const double upper = 0.8 * h->cfg.Ly, totalDY = upper - a.lower;
+    const double ds = std::fmin(h->dx, std::fmin(h->dy, h->dz));
+    const double pi = 3.14159265358979323846;
+    a.nang = num_angles;
+    for (int ap = 0; ap < num_angles; ap++) {
+        double minAngle = 0.0;
+        double ang = minAngle + ((double)ap / ((double)(num_angles - 1))) * (max_angle - minAngle);
+        ang *= pi / 180.0;
+        const double Ldiag = totalDY / std::cos(ang);
+        const double totalDX = Ldiag * std::sin(ang);
+        const int nl = (int)std::ceil(Ldiag / ds) + 1;
+        a.nline[ap] = nl;
+        a.dsl[ap] = Ldiag / (double)(nl - 1);
+        a.dxl[ap] = totalDX / (double)(nl - 1);
+        a.dyl[ap] = totalDY / (double)(nl - 1);
+    }
+    a.out = h->aero_buf;
+    CS3D_CUDA(launch_aero(a, h->stream));
+    h->launches++;
+    CS3D_CUDA(cudaMemcpyAsync(opl, h->aero_buf, n * 8, cudaMemcpyDeviceToHost, h->stream));
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }

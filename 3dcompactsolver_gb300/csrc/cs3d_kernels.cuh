@@ -180,6 +180,18 @@ constexpr int kTurbSums = 11;
 template <typename T>
 cudaError_t launch_turb(const DiagArgs<T> &a, int blocks, int pass, cudaStream_t s);
 cudaError_t launch_shear_info(const DiagArgs<double> &a, cudaStream_t s);
+// AeroOptics::computeAO: one warp per (angle, k, i) ray
+constexpr int kAeroMaxAngles = 64;
+struct AeroArgs {
+    Geom g;
+    const double *rho;
+    double Lx, Ly, Lz, dx, dy, dz, lower;
+    int nang;
+    int nline[kAeroMaxAngles];
+    double dsl[kAeroMaxAngles], dxl[kAeroMaxAngles], dyl[kAeroMaxAngles];
+    double *out;  // [nang][Nz][Nx]
+};
+cudaError_t launch_aero(const AeroArgs &a, cudaStream_t s);
 // allocation-free kinetic energy: kKeBlocks partials + the sum in a static
 // device array whose address ke_scratch_address returns
 constexpr int kKeBlocks = 1024;

@@ -530,6 +530,70 @@ cudaError_t launch_shear_info(const DiagArgs<double> &a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------
+// AeroOptics::computeAO (AeroOptics.cpp:45-93): trapezoidal integrals of the
+// density along tilted rays, trilinear interpolation as linearInterpolation
+// (Utils.cpp:261-331) with the base index kept at most N-2 (the reference
+// reads one plane past its arrays for a point exactly on the last plane,
+// where that plane's weight is 0).  Grid coordinates as Domain
+// (x_i = i/(N-1) * L).  One warp per ray; the lanes take every 32nd sample.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double grid_coord(int i, int N, double L) { return ((double)i / ((double)N - 1.0)) * L; }
+
+__device__ double aero_interp(const AeroArgs &a, const double xp[3]) {
+    const int Nx = a.g.Nx, Ny = a.g.Ny, Nz = a.g.Nz;
+    int b0 = min((int)(xp[0] / a.dx), Nx - 2);
+    int b1 = min((int)(xp[1] / a.dy), Ny - 2);
+    int b2 = min((int)(xp[2] / a.dz), Nz - 2);
+    const double x0 = grid_coord(b0, Nx, a.Lx), x1 = grid_coord(b0 + 1, Nx, a.Lx);
+    const double y0 = grid_coord(b1, Ny, a.Ly), y1 = grid_coord(b1 + 1, Ny, a.Ly);
+    const double z0 = grid_coord(b2, Nz, a.Lz), z1 = grid_coord(b2 + 1, Nz, a.Lz);
+    const double xd = (xp[0] - x0) / (x1 - x0), yd = (xp[1] - y0) / (y1 - y0), zd = (xp[2] - z0) / (z1 - z0);
+    const long long sy = Nx, sz = (long long)Nx * Ny;
+    const long long i000 = b2 * sz + b1 * sy + b0;
+    const double *f = a.rho;
+    const double c000 = f[i000], c001 = f[i000 + sz], c010 = f[i000 + sy], c011 = f[i000 + sy + sz];
+    const double c100 = f[i000 + 1], c101 = f[i000 + 1 + sz], c110 = f[i000 + 1 + sy], c111 = f[i000 + 1 + sy + sz];
+    const double c00 = c000 * (1 - xd) + c100 * xd;
+    const double c01 = c001 * (1 - xd) + c101 * xd;
+    const double c10 = c010 * (1 - xd) + c110 * xd;
+    const double c11 = c011 * (1 - xd) + c111 * xd;
+    const double c0 = c00 * (1 - yd) + c10 * yd;
+    const double c1 = c01 * (1 - yd) + c11 * yd;
+    return c0 * (1 - zd) + c1 * zd;
+}
+
+__global__ void k_aero(AeroArgs a) {
+    const int lane = threadIdx.x & 31;
+    const long long nray = (long long)a.nang * a.g.Nz * a.g.Nx;
+    for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nray;
+         r += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const int i = (int)(r % a.g.Nx);
+        const int k = (int)((r / a.g.Nx) % a.g.Nz);
+        const int ap = (int)(r / ((long long)a.g.Nx * a.g.Nz));
+        const int nl = a.nline[ap];
+        const double dsl = a.dsl[ap], dxl = a.dxl[ap], dyl = a.dyl[ap];
+        const double xi = grid_coord(i, a.g.Nx, a.Lx), zk = grid_coord(k, a.g.Nz, a.Lz);
+        double acc = 0.0;
+        for (int sp = lane; sp < nl; sp += 32) {
+            const double xp[3] = {fmod(xi + (double)(sp * dxl), a.Lx), a.lower + (double)(sp * dyl), zk};
+            const double v = aero_interp(a, xp);
+            acc += (sp == 0 || sp == nl - 1) ? v * dsl / 2.0 : v * dsl;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) a.out[r] = acc;
+    }
+}
+
+cudaError_t launch_aero(const AeroArgs &a, cudaStream_t s) {
+    const long long nray = (long long)a.nang * a.g.Nz * a.g.Nx;
+    long long blocks = (nray * 32 + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_aero<<<(unsigned)blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
 // Kinetic energy without any allocation: the KEsum column of the
 // Taylor-Green diagnostics (CSolver_AWS.cpp:2175-2236) from four device
 // arrays, with its partial sums in a fixed file-scope scratch array instead

@@ -219,6 +219,18 @@ int cs3d_turbulence_quantities(cs3d_handle *h, double out[11]);
  * reference only on steps that are multiples of 25). */
 int cs3d_shear_layer_info(cs3d_handle *h, double *out);
 
+/* AeroOptics::computeAO (AeroOptics.cpp:3-93, Utils.cpp:242-331): for
+ * num_angles beam angles 0 .. max_angle degrees (the reference uses 5 and
+ * 70) and every x-z position, the trapezoidal integral of the density along
+ * a ray from y = 0.2 Ly to 0.8 Ly tilted by the angle in x (periodic in x),
+ * trilinear interpolation at spacing about min(dx, dy, dz).
+ * opl[ap*Nx*Nz + k*Nx + i] (the contents of the reference's <angle>.OPL
+ * rows).  The density is that of the current state q1; the reference
+ * integrates rho2, which equals it on steps without filtering and holds
+ * filterConservedData's transposition scratch after filtered steps
+ * (CSolver_AWS.cpp:1697-1710). */
+int cs3d_aero_optics(cs3d_handle *h, int num_angles, double max_angle, double *opl);
+
 /* ---- restart files ------------------------------------------------------
  * dumpSolution's format (CSolver_AWS.cpp:2493-2535): the conserved state q1
  * as five raw FP64 files in XYZ order with no header, named

@@ -1191,6 +1191,81 @@ void or_shear_layer_info(or_solver *s, double *out) {
             }
 }
 
+/* linearInterpolation with getBaseNodeIndex (Utils.cpp:242-331), the base
+ * index kept at most N-2 per direction (the reference would read one plane
+ * past its arrays when a point lies exactly on the last plane, where its
+ * weight for that plane is 0). */
+static double ao_interp(const or_solver *s, const double *f, const double xp[3]) {
+    int b[3];
+    b[0] = (int)(xp[0] / s->dx);
+    b[1] = (int)(xp[1] / s->dy);
+    b[2] = (int)(xp[2] / s->dz);
+    if (b[0] > s->Nx - 2) b[0] = s->Nx - 2;
+    if (b[1] > s->Ny - 2) b[1] = s->Ny - 2;
+    if (b[2] > s->Nz - 2) b[2] = s->Nz - 2;
+    double x0 = s->x[b[0]], x1 = s->x[b[0] + 1], y0 = s->y[b[1]], y1 = s->y[b[1] + 1];
+    double z0 = s->z[b[2]], z1 = s->z[b[2] + 1];
+    double xd = (xp[0] - x0) / (x1 - x0), yd = (xp[1] - y0) / (y1 - y0), zd = (xp[2] - z0) / (z1 - z0);
+    int i = b[0], j = b[1], k = b[2];
+    double c000 = f[IDX(i, j, k)], c001 = f[IDX(i, j, k + 1)], c010 = f[IDX(i, j + 1, k)];
+    double c011 = f[IDX(i, j + 1, k + 1)], c100 = f[IDX(i + 1, j, k)], c101 = f[IDX(i + 1, j, k + 1)];
+    double c110 = f[IDX(i + 1, j + 1, k)], c111 = f[IDX(i + 1, j + 1, k + 1)];
+    double c00 = c000 * (1 - xd) + c100 * xd;
+    double c01 = c001 * (1 - xd) + c101 * xd;
+    double c10 = c010 * (1 - xd) + c110 * xd;
+    double c11 = c011 * (1 - xd) + c111 * xd;
+    double c0 = c00 * (1 - yd) + c10 * yd;
+    double c1 = c01 * (1 - yd) + c11 * yd;
+    return c0 * (1 - zd) + c1 * zd;
+}
+
+/* AeroOptics::computeAO (AeroOptics.cpp:45-93) with generateBaseBeamDiff
+ * (:3-22): for each angle and x-z position, the trapezoidal integral of the
+ * density along a ray from y = 0.2 Ly to 0.8 Ly tilted by the angle in x
+ * (periodic in x), sampled at spacing about min(dx, dy, dz).
+ * OPL[ap*Nx*Nz + k*Nx + i].  The density is that of the state q1.  The
+ * reference hands its AeroOptics object rho2 (CSolver_AWS.hpp:165), which
+ * holds the state on steps without filtering; on filtered steps
+ * filterConservedData has used rho2 as a transposition buffer
+ * (CSolver_AWS.cpp:1697-1710), and the reference integrates that. */
+void or_aero_optics(or_solver *s, int numAngles, double maxAngle, double *OPL) {
+    const double *rho = s->a[A_RHO1];
+    const double Lx = s->cfg.Lx, Ly = s->cfg.Ly;
+    const double lower = 0.2 * Ly, upper = 0.8 * Ly, totalDY = upper - lower;
+    const double ds = fmin(s->dx, fmin(s->dy, s->dz));
+    const double pi = 3.14159265358979323846;
+    for (int ap = 0; ap < numAngles; ap++) {
+        double minAngle = 0.0;
+        double ang = minAngle + ((double)ap / ((double)(numAngles - 1))) * (maxAngle - minAngle);
+        ang *= pi / 180.0;
+        double Ldiag = totalDY / cos(ang);
+        double totalDX = Ldiag * sin(ang);
+        int Nline = (int)ceil(Ldiag / ds) + 1;
+        double dsLine = Ldiag / (double)(Nline - 1);
+        double dxLine = totalDX / (double)(Nline - 1);
+        double dyLine = totalDY / (double)(Nline - 1);
+#pragma omp parallel for collapse(2) schedule(static)
+        for (int k = 0; k < s->Nz; k++)
+            for (int i = 0; i < s->Nx; i++) {
+                double b[2];
+                for (int e = 0; e < 2; e++) {
+                    int sp = e == 0 ? 0 : Nline - 1;
+                    double xp[3] = {fmod(s->x[i] + (double)(sp * dxLine), Lx), lower + (double)(sp * dyLine),
+                                    s->z[k]};
+                    b[e] = ao_interp(s, rho, xp);
+                }
+                /* the reference's order: both ends, then the interior points */
+                double opl = b[0] * dsLine / 2.0 + b[1] * dsLine / 2.0;
+                for (int sp = 1; sp < Nline - 1; sp++) {
+                    double xp[3] = {fmod(s->x[i] + (double)(sp * dxLine), Lx), lower + (double)(sp * dyLine),
+                                    s->z[k]};
+                    opl += ao_interp(s, rho, xp) * dsLine;
+                }
+                OPL[(size_t)ap * s->Nx * s->Nz + (size_t)k * s->Nx + i] = opl;
+            }
+    }
+}
+
 /* Single operator on contiguous lines: kind 1/2/3 as line_apply, nlines
  * lines of length N with spacing dh. */
 void or_line_op(int kind, int bc_type, int N, double dh, double alphaF, long nlines, const double *in,

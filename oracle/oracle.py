@@ -76,6 +76,7 @@ def port_lib(flavour="strict"):
         lib.or_tgv_quantities.argtypes = [_VP, _DP]
         lib.or_turbulence_quantities.argtypes = [_VP, _DP]
         lib.or_shear_layer_info.argtypes = [_VP, _DP]
+        lib.or_aero_optics.argtypes = [_VP, ctypes.c_int, ctypes.c_double, _DP]
         lib.or_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_long, _DP, _DP]
         lib.or_num_threads.restype = ctypes.c_int
@@ -107,6 +108,7 @@ def ref_lib(flavour="strict"):
         lib.ref_turbulence_quantities.argtypes = [_VP]
         lib.ref_shear_layer_info.argtypes = [_VP]
         lib.ref_dump_solution.argtypes = [_VP]
+        lib.ref_aero_optics.argtypes = [_VP, ctypes.c_int, ctypes.c_double, _DP]
         lib.ref_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_double, _DP, _DP]
@@ -201,6 +203,12 @@ class OraclePort(_Base):
         self.lib.or_shear_layer_info(self.h, _ptr(out))
         return out
 
+    def aero_optics(self, num_angles=5, max_angle=70.0):
+        """OPL integrals of rho2, shape (num_angles, Nz, Nx)."""
+        out = np.zeros((num_angles, self.cfg.Nz, self.cfg.Nx))
+        self.lib.or_aero_optics(self.h, num_angles, max_angle, _ptr(out))
+        return out
+
 
 class RefSolver(_Base):
     """The reference's own CSolver_AWS + RK4/TVDRK3 (oracle/_ref)."""
@@ -265,6 +273,23 @@ class RefSolver(_Base):
             os.chdir(d)
             try:
                 self.lib.ref_dump_solution(self.h)
+                return {f: open(os.path.join(d, f), "rb").read() for f in os.listdir(d)}
+            finally:
+                os.chdir(cwd)
+
+    def aero_optics(self, num_angles=5, max_angle=70.0):
+        """The reference's AeroOptics::computeAO on rho2: (OPL array, {file: bytes})."""
+        out = np.zeros((num_angles, self.cfg.Nz, self.cfg.Nx))
+        files = self._in_tmpdir_bytes(lambda: self.lib.ref_aero_optics(self.h, num_angles, max_angle, _ptr(out)))
+        return out, files
+
+    def _in_tmpdir_bytes(self, fn):
+        import tempfile
+        cwd = os.getcwd()
+        with tempfile.TemporaryDirectory() as d:
+            os.chdir(d)
+            try:
+                fn()
                 return {f: open(os.path.join(d, f), "rb").read() for f in os.listdir(d)}
             finally:
                 os.chdir(cwd)

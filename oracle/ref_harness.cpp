@@ -215,6 +215,17 @@ void ref_dump_solution(void *hp) {
     h->ts->dumpStep = ds;
 }
 
+// AeroOptics::computeAO on rho2, the field the solver hands its AeroOptics
+// object (CSolver_AWS.hpp:165); it also writes <angle>.OPL files to the
+// current directory.
+void ref_aero_optics(void *hp, int num_angles, double max_angle, double *out) {
+    RefHandle *h = (RefHandle *)hp;
+    AeroOptics ao(h->dom, h->cs->ig, h->cs->rho2, h->cs->p, h->cs->T, num_angles, max_angle);
+    ao.computeAO();
+    memcpy(out, ao.OPL, sizeof(double) * (size_t)num_angles * h->dom->Nx * h->dom->Nz);
+    delete[] ao.OPL;
+}
+
 void ref_get_scalars(void *hp, double *dt, double *time, int *time_step) {
     RefHandle *h = (RefHandle *)hp;
     *dt = h->ts->dt;

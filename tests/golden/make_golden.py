@@ -9,6 +9,7 @@ and the reference harness built by `make -C oracle ref`.  Writes:
                                (oracle/_ref, strict build), with dt, time and timeStep
   ref_diagnostics.npz          the reference's calcTurbulenceQuantities row and shearLayerInfoCalc
                                profiles after 2 steps + the stages of a third (before postStep's sponge)
+  ref_aero.npz                 the reference's AeroOptics::computeAO OPL after 3 unfiltered steps
   ref_lineops.npz              the reference's calc1stDerivField / calc2ndDerivField /
                                filterField on seeded random fields
 
@@ -41,6 +42,8 @@ CASES = {
 NSTEPS = 3
 DIAG_EXTRA = {"hit12": lambda: cases.hit(12, seed=3, k0=3.0)}
 DIAG_CASES = ["tgv12", "hit12", "shear", "wall_moving_sponge"]
+AERO_CASES = {"shear": lambda: cases.shear_layer(16, 12, 10, precision=_abi.FP64),
+              "tgv12_nofilter": lambda: cases.tgv(12, filter_step=1000)}
 
 # single operators: (kind, dir, bc_type, (Nx, Ny, Nz))
 LINEOPS = [(k, d, bc, n) for k in (1, 2, 3) for d in (0, 1, 2) for bc in (0, 1)
@@ -80,6 +83,17 @@ def main():
         diag[f"{name}_turb"] = r.turbulence_quantities()
         diag[f"{name}_shear"] = r.shear_layer_info()
     np.savez_compressed(os.path.join(HERE, "ref_diagnostics.npz"), **diag)
+    # the reference's AeroOptics::computeAO (5 angles up to 70 degrees) after 3
+    # steps without filtering, where its rho2 holds the state
+    aero = {}
+    for name, mk in AERO_CASES.items():
+        cfg, ic = mk()
+        r = oracle.RefSolver(cfg)
+        r.set_initial_conditions(*ic)
+        for _ in range(3):
+            r.step()
+        aero[name], _ = r.aero_optics(5, 70.0)
+    np.savez_compressed(os.path.join(HERE, "ref_aero.npz"), **aero)
     rng = np.random.default_rng(2024)
     out = {}
     for idx, (kind, d, bc, n) in enumerate(LINEOPS):

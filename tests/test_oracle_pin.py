@@ -177,3 +177,29 @@ def test_reference_dump_format(oracle, cases):
         data = np.frombuffer(files[f"{n}.out.3"], dtype="<f8")
         assert data.size == cfg.npts
         assert np.array_equal(data, r.get(["rho1", "rhoU1", "rhoV1", "rhoW1", "rhoE1"][f]).reshape(-1))
+
+
+AERO_CASES = ["shear", "tgv12_nofilter"]
+
+
+def aero_case(cases, name):
+    import importlib
+    _abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    if name == "shear":
+        return cases.shear_layer(16, 12, 10, precision=_abi.FP64)
+    if name == "tgv12_nofilter":
+        return cases.tgv(12, filter_step=1000)
+    return cases.tgv(12)
+
+
+@pytest.mark.parametrize("name", AERO_CASES)
+def test_port_aero_optics_matches_reference(oracle, cases, name):
+    """AeroOptics::computeAO after 3 steps without filtering (where the
+    reference's rho2 is the state): the restatement bit for bit on x86-64."""
+    g = load_golden("ref_aero.npz")
+    cfg, ic = aero_case(cases, name)
+    p = oracle.OraclePort(cfg)
+    p.set_initial_conditions(*ic)
+    p.run(3)
+    tol = 0.0 if platform.machine() == "x86_64" else 1e-14
+    assert rel_err(p.aero_optics(5, 70.0), g[name]) <= tol
