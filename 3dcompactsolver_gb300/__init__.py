@@ -77,6 +77,7 @@ def lib():
         L.cs3d_turbulence_quantities.argtypes = [_H, _DP]
         L.cs3d_dump_solution.argtypes = [_H, ctypes.c_char_p]
         L.cs3d_aero_optics.argtypes = [_H, ctypes.c_int, ctypes.c_double, _DP]
+        L.cs3d_vorticity_q.argtypes = [_H, _DP, _DP]
         L.cs3d_load_solution.argtypes = [_H, ctypes.c_char_p, ctypes.c_int, ctypes.c_double]
         L.cs3d_shear_layer_info.argtypes = [_H, _DP]
         L.cs3d_kernel_times.argtypes = [_H, _DP, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
@@ -227,6 +228,13 @@ class Solver:
         sp = _dptr(keep) if keep is not None else None
         check(lib().cs3d_adjoint_backward(self.h, int(objective), sp, _dptr(grad), ctypes.byref(J)))
         return grad, J.value
+
+    def vorticity_q(self):
+        """(|curl u|, Q-criterion) of the current state, each (Nz, Ny, Nx)."""
+        v = np.empty(self.shape)
+        q = np.empty(self.shape)
+        check(lib().cs3d_vorticity_q(self.h, _dptr(v), _dptr(q)))
+        return v, q
 
     def aero_optics(self, num_angles=5, max_angle=70.0):
         """Optical-path integrals of the density, shape (num_angles, Nz, Nx)."""

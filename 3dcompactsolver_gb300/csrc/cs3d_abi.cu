@@ -338,6 +338,7 @@ struct cs3d_handle {
     double *prim_out = nullptr;  // 7 FP64 fields for cs3d_get_field of primitives
     double *red = nullptr;       // reduction scratch
     double *shear_buf = nullptr; // 17 x Ny per-plane statistics
+    double *post_buf = nullptr;  // 14 FP64 fields of the post-processor
     double *aero_buf = nullptr;  // optical path integrals
     size_t aero_cap = 0;
     std::vector<void *> allocs;
@@ -1932,6 +1933,49 @@ extern "C" int cs3d_load_solution(cs3d_handle *h, const char *prefix, int time_s
     h->filterTimeStep = time_step / h->cfg.filter_step;  // filtered steps so far
     double sc[2] = {0.0, time};
     CS3D_CUDA(cudaMemcpyAsync(h->scal, sc, 2 * 8, cudaMemcpyHostToDevice, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
+// post-processor: vorticity magnitude and Q-criterion (PostProcess.cpp:190-310)
+// ---------------------------------------------------------------------
+extern "C" int cs3d_vorticity_q(cs3d_handle *h, double *vort, double *qcrit) {
+    if (!h || !vort || !qcrit) return fail(CS3D_ERR_ARG, "null argument");
+    if (!h->ic_done) return fail(CS3D_ERR_STATE, "cs3d_set_initial_conditions has not been called");
+    DeviceGuard dg(h->dev);
+    const size_t n = (size_t)h->g.npts;
+    if (!h->post_buf) {
+        int rc = dalloc(h, (void **)&h->post_buf, 14 * n * 8);
+        if (rc) return rc;
+    }
+    PostArgs a{};
+    a.g = h->g;
+    a.q = h->q1;
+    double *d[3][3];
+    for (int c = 0; c < 3; c++) {
+        a.vel[c] = h->post_buf + (size_t)c * n;
+        for (int e = 0; e < 3; e++) {
+            d[c][e] = h->post_buf + (size_t)(3 + 3 * c + e) * n;
+            a.d[c][e] = d[c][e];
+        }
+    }
+    a.vort = h->post_buf + 12 * n;
+    a.qcrit = h->post_buf + 13 * n;
+    CS3D_CUDA(launch_velocity(a, h->stream));
+    h->launches++;
+    // the nine first derivatives with the solver's FP64 operators, one launch per direction
+    for (int e = 0; e < 3; e++) {
+        int rc = adj_apply<double>(h, e, 0, 1,
+                                   {{a.vel[0], nullptr, d[0][e], nullptr, 1.0, 0, 0},
+                                    {a.vel[1], nullptr, d[1][e], nullptr, 1.0, 0, 0},
+                                    {a.vel[2], nullptr, d[2][e], nullptr, 1.0, 0, 0}});
+        if (rc) return rc;
+    }
+    CS3D_CUDA(launch_vort_q(a, h->stream));
+    h->launches++;
+    CS3D_CUDA(cudaMemcpyAsync(vort, a.vort, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaMemcpyAsync(qcrit, a.qcrit, n * 8, cudaMemcpyDeviceToHost, h->stream));
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     return CS3D_OK;
 }

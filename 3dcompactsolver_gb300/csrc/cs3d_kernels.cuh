@@ -192,6 +192,17 @@ struct AeroArgs {
     double *out;  // [nang][Nz][Nx]
 };
 cudaError_t launch_aero(const AeroArgs &a, cudaStream_t s);
+// post-processor: velocity of q1, then |curl u| and the Q-criterion from the
+// nine first derivatives d[c][e] = d(u_c)/d(x_e)
+struct PostArgs {
+    Geom g;
+    Q5 q;
+    double *vel[3];
+    const double *d[3][3];
+    double *vort, *qcrit;
+};
+cudaError_t launch_velocity(const PostArgs &a, cudaStream_t s);
+cudaError_t launch_vort_q(const PostArgs &a, cudaStream_t s);
 // allocation-free kinetic energy: kKeBlocks partials + the sum in a static
 // device array whose address ke_scratch_address returns
 constexpr int kKeBlocks = 1024;

@@ -594,6 +594,50 @@ cudaError_t launch_aero(const AeroArgs &a, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------
+// post-processor (PostProcess.cpp:190-310): U, V, W of q1, then per point the
+// vorticity magnitude and Q = |W|^2/2 - |S|^2/2, S and W the symmetric and
+// antisymmetric parts of the velocity gradient, summed in the reference's
+// order
+// ---------------------------------------------------------------------
+__global__ void k_velocity(PostArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        const double r = a.q.f[0][gi];
+        a.vel[0][gi] = a.q.f[1][gi] / r;
+        a.vel[1][gi] = a.q.f[2][gi] / r;
+        a.vel[2][gi] = a.q.f[3][gi] / r;
+    }
+}
+
+__global__ void k_vort_q(PostArgs a) {
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+         gi += (long long)gridDim.x * blockDim.x) {
+        const double Ux = a.d[0][0][gi], Uy = a.d[0][1][gi], Uz = a.d[0][2][gi];
+        const double Vx = a.d[1][0][gi], Vy = a.d[1][1][gi], Vz = a.d[1][2][gi];
+        const double Wx = a.d[2][0][gi], Wy = a.d[2][1][gi], Wz = a.d[2][2][gi];
+        const double vx = Wy - Vz, vy = Uz - Wx, vz = Vx - Uy;
+        a.vort[gi] = sqrt(vx * vx + vy * vy + vz * vz);
+        const double s01 = 0.5 * (Uy + Vx), s12 = 0.5 * (Vz + Wy), s02 = 0.5 * (Uz + Wx);
+        const double w01 = 0.5 * (Uy - Vx), w12 = 0.5 * (Vz - Wy), w02 = 0.5 * (Uz - Wx);
+        // the nine products of each tensor in row order, as the reference sums them
+        const double om2 = 0.5 * (0.0 * 0.0 + w01 * w01 + w02 * w02 + (-w01) * (-w01) + 0.0 * 0.0 + w12 * w12 +
+                                  (-w02) * (-w02) + (-w12) * (-w12) + 0.0 * 0.0);
+        const double st2 = 0.5 * (Ux * Ux + s01 * s01 + s02 * s02 + s01 * s01 + Vy * Vy + s12 * s12 + s02 * s02 +
+                                  s12 * s12 + Wz * Wz);
+        a.qcrit[gi] = om2 - st2;
+    }
+}
+
+cudaError_t launch_velocity(const PostArgs &a, cudaStream_t s) {
+    k_velocity<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_vort_q(const PostArgs &a, cudaStream_t s) {
+    k_vort_q<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
 // Kinetic energy without any allocation: the KEsum column of the
 // Taylor-Green diagnostics (CSolver_AWS.cpp:2175-2236) from four device
 // arrays, with its partial sums in a fixed file-scope scratch array instead

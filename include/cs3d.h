@@ -231,6 +231,14 @@ int cs3d_shear_layer_info(cs3d_handle *h, double *out);
  * (CSolver_AWS.cpp:1697-1710). */
 int cs3d_aero_optics(cs3d_handle *h, int num_angles, double max_angle, double *opl);
 
+/* The post-processor's vorticity magnitude and Q-criterion
+ * (PostProcess.cpp:190-310) for the current state q1 (load a dump with
+ * cs3d_load_solution first to post-process one): U = rhoU/rho, ..., the nine
+ * first derivatives with the solver's FP64 compact operators, then per point
+ * vort = |curl u| and qcrit = |W|^2/2 - |S|^2/2 (S, W: symmetric and
+ * antisymmetric parts of grad u).  vort and qcrit: npts host doubles each. */
+int cs3d_vorticity_q(cs3d_handle *h, double *vort, double *qcrit);
+
 /* ---- restart files ------------------------------------------------------
  * dumpSolution's format (CSolver_AWS.cpp:2493-2535): the conserved state q1
  * as five raw FP64 files in XYZ order with no header, named

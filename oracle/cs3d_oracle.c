@@ -1266,6 +1266,50 @@ void or_aero_optics(or_solver *s, int numAngles, double maxAngle, double *OPL) {
     }
 }
 
+/* The vorticity magnitude and Q-criterion of the post-processor
+ * (PostProcess.cpp:190-310) for the state q1: U, V, W = rhoU/rho, ...; the
+ * nine first derivatives with the solver's operators; per point
+ * |curl u| and Q = |W|^2/2 - |S|^2/2 with S and W the symmetric and
+ * antisymmetric parts of grad u. */
+void or_vorticity_q(or_solver *s, double *vort, double *qcrit) {
+    const size_t n = s->N;
+    double *vel[3], *d[3][3];
+    for (int c = 0; c < 3; c++) {
+        vel[c] = (double *)malloc(n * sizeof(double));
+        for (int e = 0; e < 3; e++) d[c][e] = (double *)malloc(n * sizeof(double));
+    }
+    for (size_t ip = 0; ip < n; ip++)
+        for (int c = 0; c < 3; c++) vel[c][ip] = s->a[A_RHOU1 + c][ip] / s->a[A_RHO1][ip];
+    for (int c = 0; c < 3; c++)
+        for (int e = 0; e < 3; e++) field_apply(s, e, 1, vel[c], d[c][e]);
+#pragma omp parallel for schedule(static)
+    for (long ip = 0; ip < (long)n; ip++) {
+        double Ux = d[0][0][ip], Uy = d[0][1][ip], Uz = d[0][2][ip];
+        double Vx = d[1][0][ip], Vy = d[1][1][ip], Vz = d[1][2][ip];
+        double Wx = d[2][0][ip], Wy = d[2][1][ip], Wz = d[2][2][ip];
+        double vx = Wy - Vz, vy = Uz - Wx, vz = Vx - Uy;
+        vort[ip] = sqrt(vx * vx + vy * vy + vz * vz);
+        double sij[3][3], wij[3][3];
+        sij[0][0] = Ux; sij[1][1] = Vy; sij[2][2] = Wz;
+        sij[0][1] = 0.5 * (Uy + Vx); sij[1][2] = 0.5 * (Vz + Wy); sij[0][2] = 0.5 * (Uz + Wx);
+        wij[0][0] = 0.0; wij[1][1] = 0.0; wij[2][2] = 0.0;
+        wij[0][1] = 0.5 * (Uy - Vx); wij[1][2] = 0.5 * (Vz - Wy); wij[0][2] = 0.5 * (Uz - Wx);
+        sij[1][0] = sij[0][1]; sij[2][1] = sij[1][2]; sij[2][0] = sij[0][2];
+        wij[1][0] = -wij[0][1]; wij[2][1] = -wij[1][2]; wij[2][0] = -wij[0][2];
+        double om2 = 0.5 * (wij[0][0] * wij[0][0] + wij[0][1] * wij[0][1] + wij[0][2] * wij[0][2] +
+                            wij[1][0] * wij[1][0] + wij[1][1] * wij[1][1] + wij[1][2] * wij[1][2] +
+                            wij[2][0] * wij[2][0] + wij[2][1] * wij[2][1] + wij[2][2] * wij[2][2]);
+        double st2 = 0.5 * (sij[0][0] * sij[0][0] + sij[0][1] * sij[0][1] + sij[0][2] * sij[0][2] +
+                            sij[1][0] * sij[1][0] + sij[1][1] * sij[1][1] + sij[1][2] * sij[1][2] +
+                            sij[2][0] * sij[2][0] + sij[2][1] * sij[2][1] + sij[2][2] * sij[2][2]);
+        qcrit[ip] = om2 - st2;
+    }
+    for (int c = 0; c < 3; c++) {
+        free(vel[c]);
+        for (int e = 0; e < 3; e++) free(d[c][e]);
+    }
+}
+
 /* Single operator on contiguous lines: kind 1/2/3 as line_apply, nlines
  * lines of length N with spacing dh. */
 void or_line_op(int kind, int bc_type, int N, double dh, double alphaF, long nlines, const double *in,

@@ -77,6 +77,7 @@ def port_lib(flavour="strict"):
         lib.or_turbulence_quantities.argtypes = [_VP, _DP]
         lib.or_shear_layer_info.argtypes = [_VP, _DP]
         lib.or_aero_optics.argtypes = [_VP, ctypes.c_int, ctypes.c_double, _DP]
+        lib.or_vorticity_q.argtypes = [_VP, _DP, _DP]
         lib.or_line_op.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_long, _DP, _DP]
         lib.or_num_threads.restype = ctypes.c_int
@@ -203,8 +204,15 @@ class OraclePort(_Base):
         self.lib.or_shear_layer_info(self.h, _ptr(out))
         return out
 
+    def vorticity_q(self):
+        """(|curl u|, Q-criterion) of the state, each (Nz, Ny, Nx)."""
+        v = np.zeros(self.shape)
+        q = np.zeros(self.shape)
+        self.lib.or_vorticity_q(self.h, _ptr(v), _ptr(q))
+        return v, q
+
     def aero_optics(self, num_angles=5, max_angle=70.0):
-        """OPL integrals of rho2, shape (num_angles, Nz, Nx)."""
+        """OPL integrals of the density of q1, shape (num_angles, Nz, Nx)."""
         out = np.zeros((num_angles, self.cfg.Nz, self.cfg.Nx))
         self.lib.or_aero_optics(self.h, num_angles, max_angle, _ptr(out))
         return out
