@@ -35,8 +35,11 @@
 #include <cmath>
 #include "cs3d_tile.cuh"
 
-#ifndef CS3D_ZBC
-#define CS3D_ZBC 2     // points per thread in flight in the z sweep's consume phase
+#ifndef CS3D_ZC1
+#define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
+#endif
+#ifndef CS3D_ZC2
+#define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
 #endif
 // Resident blocks per SM the mixed-form sweeps are compiled for (256 threads
 // each: x at 3 blocks / 80 registers, y and z at 2 blocks / 128 registers
@@ -292,16 +295,20 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
     const bool use_q1a = tvd || st == 1;
     const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
     const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
-    const bool need_qs = a.sponge || (a.mixed_rk4 && st == 1);
-    struct InC {
+    const bool need_qs = a.mixed_rk4 && st == 1;
+    // Phase C runs in two passes over the same points, each point by the same
+    // thread in both (so no barrier between them): C1 forms the right-hand
+    // side and parks dq = dt*RHS in the point's own, now unused, solve slots;
+    // C2 streams the FP64 state through the RK update.  Each pass keeps fewer
+    // values live than one fused pass, so more points' loads are in flight.
+    constexpr int kDq[5] = {ZS, ZWX, ZWY, ZRW, ZF1};
+    struct InC1 {
         Pt pt;
         T v[18];
-        double qa[5], qb[5];
         T qsv[5];
-        float q1f[5];
     };
-    pipelined<InC>(NL,
-        [&](InC &in, int p) {
+    batched<InC1, CS3D_ZC1>(NL,
+        [&](InC1 &in, int p) {
             in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
             in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi];
@@ -311,13 +318,10 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
                 in.v[13 + f] = a.R[f][gi];
-                in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
-                in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
-                in.q1f[f] = need_q1s ? a.q1s[f][gi] : 0.f;
-                in.qsv[f] = need_qs ? a.qs[f][gi] : T(0);
+                in.qsv[f] = a.sponge ? a.qs[f][gi] : T(0);
             }
         },
-        [&](InC &in) {
+        [&](InC1 &in) {
             if (!in.pt.ok) return;
             const Pt &p = in.pt;
             const unsigned gi = p.gi;
@@ -372,13 +376,41 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
             if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
                 a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
             }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                // plain form: dq = dt * RHS in FP64; mixed form: in FP32
+                T d = sizeof(T) == 8 ? (T)(dt * (double)R[f]) : dtw * R[f];
+                if (zero_all || (f > 0 && zero_mom)) d = T(0);
+                if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
+                sm.b(kDq[f])[p.o] = d;
+            }
+        });
+    struct InC2 {
+        Pt pt;
+        double qa[5], qb[5];
+        T qsv[5];
+        float q1f[5];
+    };
+    batched<InC2, CS3D_ZC2>(NL,
+        [&](InC2 &in, int p) {
+            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
+                in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
+                in.q1f[f] = need_q1s ? a.q1s[f][gi] : 0.f;
+                in.qsv[f] = need_qs ? a.qs[f][gi] : T(0);
+            }
+        },
+        [&](InC2 &in) {
+            if (!in.pt.ok) return;
+            const unsigned gi = in.pt.gi;
             if (sizeof(T) == 8) {
-                // plain form: dq = dt * RHS and the reference's RK update in FP64
+                // plain form: the reference's RK update in FP64
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    double d = dt * (double)R[f];
-                    if (zero_all || (f > 0 && zero_mom)) d = 0.0;
-                    if (a.dq_out[0]) a.dq_out[f][gi] = d;
+                    const double d = (double)sm.b(kDq[f])[in.pt.o];
                     if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
                         if (st == 1) a.qk.f[f][gi] = in.qa[f] + d;
                         else if (st == 2) a.qk.f[f][gi] = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * d;
@@ -392,13 +424,10 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
                     }
                 }
             } else {
-                // mixed form: the increment dq = dt*RHS in FP32; the conserved
-                // state accumulates it in FP64
+                // mixed form: the FP32 increment accumulated into the FP64 state
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    T d = dtw * R[f];
-                    if (zero_all || (f > 0 && zero_mom)) d = T(0);
-                    if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
+                    const T d = sm.b(kDq[f])[in.pt.o];
                     if (tvd) {
                         const double dd = to_f64(d);
                         double nv;
