@@ -673,6 +673,7 @@ static int launch_cfl_reduce(cs3d_handle *h) {
     if (h->mixed)
         for (int f = 0; f < 5; f++) a.qs[f] = h->q1s[f];
     a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
+    a.idx = (float)(1.0 / h->dx); a.idy = (float)(1.0 / h->dy); a.idz = (float)(1.0 / h->dz);
     a.max_out = h->scal + 2;
     a.nan_flag = h->flag;
     tstart(h, CS3D_K_CFL);

@@ -95,7 +95,7 @@ __global__ void k_cfl(CflArgs a) {
     if (a.qs[0]) {
         float fm = 0.f;
         const float gam = (float)a.gas.gamma, gm1 = (float)a.gas.gm1;
-        const float idx = (float)(1.0 / a.dx), idy = (float)(1.0 / a.dy), idz = (float)(1.0 / a.dz);
+        const float idx = a.idx, idy = a.idy, idz = a.idz;
         for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
              gi += (long long)gridDim.x * blockDim.x) {
             const float r = a.qs[0][gi];
@@ -136,7 +136,11 @@ __global__ void k_finalize_dt(DtArgs a) {
 // updateSponge (CSolver_AWS.cpp:1937-2031)
 // ---------------------------------------------------------------------
 __global__ void k_sponge_update(SpongeArgs a) {
-    const double eps = 1.0 / (a.avgT / *a.dt + 1.0);
+    // the averaging weight, once per block (FP64 divisions are slow)
+    __shared__ double eps_s;
+    if (threadIdx.x == 0) eps_s = 1.0 / (a.avgT / *a.dt + 1.0);
+    __syncthreads();
+    const double eps = eps_s;
     const long long nxy = (long long)a.g.Nx * a.g.Ny;
     for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
          gi += (long long)gridDim.x * blockDim.x) {
