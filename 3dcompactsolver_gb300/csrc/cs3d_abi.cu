@@ -479,9 +479,9 @@ static int check_config(const cs3d_config *c) {
 // y and z sweeps of the mixed form at N = 128 this gives 8 lines: every
 // global access is then a full 32-byte sector, which measured faster than
 // narrower tiles with more blocks per SM.  CS3D_SMEM_BUDGET_KB overrides it.
-static int pick_L(size_t tb, int nbuf, int N, int pitch_plus) {
+static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, const char *env = "CS3D_SMEM_BUDGET_KB") {
     size_t budget = 72 * 1024;
-    if (const char *e = getenv("CS3D_SMEM_BUDGET_KB")) {
+    if (const char *e = getenv(env)) {
         long v = strtol(e, nullptr, 10);
         if (v >= 8 && v <= 220) budget = (size_t)v * 1024;
     }
@@ -610,7 +610,7 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         }
     for (int d = 0; d < 3; d++) {
         h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
-        h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0);
+        h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB");
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
@@ -884,7 +884,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                 fa.lgL = ilog2(h->Lf[d]);
                 fa.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
                 fa.P = h->Lf[d] + (d == 0 ? 1 : 0);
-                fa.threads = 128;
+                fa.threads = sizeof(T) == 4 ? filter_threads<float>() : filter_threads<double>();
                 if (sizeof(T) == 8) fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][2].op);
                 else fa.op = *reinterpret_cast<const LineOp<T> *>(&h->op32fc[d].op);
                 void **src = pass == 1 ? h->ft1 : h->ft2;

@@ -13,6 +13,12 @@ namespace cs3d {
 template <typename T>
 __host__ __device__ constexpr int sweep_threads() { return sizeof(T) == 4 ? CS3D_TPB : 128; }
 
+#ifndef CS3D_FTPB
+#define CS3D_FTPB 256  // threads per block of the mixed-form filter
+#endif
+template <typename T>
+__host__ __device__ constexpr int filter_threads() { return sizeof(T) == 4 ? CS3D_FTPB : 128; }
+
 // Ideal-gas constants (IdealGas.hpp:36-46).
 struct GasParams {
     double gamma;   // 1.4

@@ -35,6 +35,9 @@
 #include <cmath>
 #include "cs3d_tile.cuh"
 
+#ifndef CS3D_FB
+#define CS3D_FB 4      // points per thread in flight in the mixed filter's load and store loops
+#endif
 #ifndef CS3D_ZC1
 #define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
 #endif
@@ -466,8 +469,8 @@ __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2
 __constant__ Task kTasksFc[3] = {{0, 5, 2, 1, 6, 2}, {2, 7, 2, 3, 8, 2}, {4, 9, 2, 4, 9, 2}};
 
 template <typename T, int DIR>
-__global__ void __launch_bounds__(128) k_filter(FilterArgs<T> a) {
-    constexpr int B = 2;
+__global__ void __launch_bounds__(filter_threads<T>()) k_filter(FilterArgs<T> a) {
+    constexpr int B = sizeof(T) == 4 ? CS3D_FB : 2;
     constexpr bool kCorr = sizeof(T) == 4;
     const int L = a.L, P = a.P;
     const Tile t = make_tile<DIR>(a.g, L);
