@@ -28,6 +28,19 @@ __device__ __forceinline__ double temp_at(const BCArgs &a, long long gi, int fc)
     return p / (r * a.gas.R);
 }
 
+// The same temperature in FP32 from the FP32 shadow (mixed form: the stage
+// input's shadow is what the sweeps read; FP64 divisions are slow here).
+__device__ __forceinline__ float temp_at32(const BCArgs &a, long long gi, int fc) {
+    float q[5];
+    const bool bk = a.use_backup && (fc & a.sponge_faces) && !(fc & a.wall_faces);
+#pragma unroll
+    for (int f = 0; f < 5; ++f) q[f] = bk ? narrow(a.backup.f[f][gi]) : a.qs[f][gi];
+    const float r = q[0];
+    const float U = q[1] / r, V = q[2] / r, W = q[3] / r;
+    const float p = (float)a.gas.gm1 * (q[4] - 0.5f * r * (U * U + V * V + W * W));
+    return p / (r * (float)a.gas.R);
+}
+
 __global__ void k_wall_pre(BCArgs a) {
     const Geom g = a.g;
     const int dir = a.face / 2, hi = a.face % 2;
@@ -44,16 +57,30 @@ __global__ void k_wall_pre(BCArgs a) {
     const long long nxy = (long long)g.Nx * g.Ny;
     const long long gi = (long long)k * nxy + (long long)j * g.Nx + i;
     const long long step = dir == 0 ? 1 : dir == 1 ? g.Nx : nxy;
-    double Tn[6];
+    double Tw;
+    if (a.qs[0]) {  // mixed form: FP32 from the shadow
+        float Tn[6];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) {
-        const long long nb = gi + sg * (m + 1) * step;
-        int ii = i, jj = j, kk = k;
-        if (dir == 0) ii += sg * (m + 1); else if (dir == 1) jj += sg * (m + 1); else kk += sg * (m + 1);
-        Tn[m] = temp_at(a, nb, faces_of(g, ii, jj, kk));
+        for (int m = 0; m < 6; ++m) {
+            const long long nb = gi + sg * (m + 1) * step;
+            int ii = i, jj = j, kk = k;
+            if (dir == 0) ii += sg * (m + 1); else if (dir == 1) jj += sg * (m + 1); else kk += sg * (m + 1);
+            Tn[m] = temp_at32(a, nb, faces_of(g, ii, jj, kk));
+        }
+        Tw = widen((Tn[0] * 360.f - Tn[1] * 450.f + Tn[2] * 400.f - Tn[3] * 225.f + Tn[4] * 72.f - Tn[5] * 10.f) /
+                   147.f);
+    } else {
+        double Tn[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            const long long nb = gi + sg * (m + 1) * step;
+            int ii = i, jj = j, kk = k;
+            if (dir == 0) ii += sg * (m + 1); else if (dir == 1) jj += sg * (m + 1); else kk += sg * (m + 1);
+            Tn[m] = temp_at(a, nb, faces_of(g, ii, jj, kk));
+        }
+        // Utils.hpp:52-54
+        Tw = (Tn[0] * 360.0 - Tn[1] * 450.0 + Tn[2] * 400.0 - Tn[3] * 225.0 + Tn[4] * 72.0 - Tn[5] * 10.0) / 147.0;
     }
-    // Utils.hpp:52-54
-    const double Tw = (Tn[0] * 360.0 - Tn[1] * 450.0 + Tn[2] * 400.0 - Tn[3] * 225.0 + Tn[4] * 72.0 - Tn[5] * 10.0) / 147.0;
     const double r = a.q.f[0] ? a.q.f[0][gi] : widen(a.qs[0][gi]);
     double nq[5];
     nq[0] = r;
