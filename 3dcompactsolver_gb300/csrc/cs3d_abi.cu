@@ -321,7 +321,7 @@ struct cs3d_handle {
     DevOp<float> op32[3][3];
     DevOp<float> op32fc[3];  // FP32 filter correction F - I (mixed form)
     // tiles
-    int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads = 128;
+    int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads[3] = {128, 128, 128};
     // step state
     int timeStep = 0, filterTimeStep = 0;
     int ic_done = 0;
@@ -479,8 +479,9 @@ static int check_config(const cs3d_config *c) {
 // y and z sweeps of the mixed form at N = 128 this gives 8 lines: every
 // global access is then a full 32-byte sector, which measured faster than
 // narrower tiles with more blocks per SM.  CS3D_SMEM_BUDGET_KB overrides it.
-static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, const char *env = "CS3D_SMEM_BUDGET_KB") {
-    size_t budget = 72 * 1024;
+static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, const char *env = "CS3D_SMEM_BUDGET_KB",
+                  int budget_kb = 72) {
+    size_t budget = (size_t)budget_kb * 1024;
     if (const char *e = getenv(env)) {
         long v = strtol(e, nullptr, 10);
         if (v >= 8 && v <= 220) budget = (size_t)v * 1024;
@@ -609,15 +610,29 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             if (r) return fail_free(r);
         }
     for (int d = 0; d < 3; d++) {
+        // Tile shape.  Default: the widest tile within 72 kB (x: 3 blocks of
+        // 256 per SM; y, z: 2 blocks of 256).  A mixed-form y or z tile
+        // narrower than 16 lines there (z rows of 32 bytes or less per field)
+        // instead takes one block of 512 threads per SM and the widest tile
+        // within 200 kB: measured at 128^3, z 0.79 -> 0.70 ms per step; where
+        // the 72 kB tile is already 16 lines wide (N = 42) one block per SM was
+        // slower, its phases no longer overlapping another block's.
         h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
+        h->threads[d] = h->mixed ? (d == 0 ? sweep_threads<float>(0) : 256) : sweep_threads<double>(d);
+        if (h->mixed && d > 0 && h->L[d] < 16 && !getenv("CS3D_SMEM_BUDGET_KB")) {
+            h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], 0, "CS3D_SMEM_BUDGET_KB", 200);
+            h->threads[d] = sweep_threads<float>(d);
+        }
         h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB");
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
-    h->threads = h->mixed ? sweep_threads<float>() : sweep_threads<double>();
     if (const char *e = getenv("CS3D_THREADS")) {
         long v = strtol(e, nullptr, 10);
-        if (v == 64 || v == 128 || (v <= h->threads && v % 32 == 0 && v > 0)) h->threads = (int)v;
+        for (int d = 0; d < 3; d++) {
+            const int mx = h->mixed ? sweep_threads<float>(d) : sweep_threads<double>(d);
+            if (v > 0 && v <= mx && v % 32 == 0) h->threads[d] = (int)v;
+        }
     }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
@@ -812,7 +827,6 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     }
     SweepArgs<T> a{};
     a.g = h->g;
-    a.threads = h->threads;
     a.gas = h->gas;
     a.q = qin;
     for (int f = 0; f < 5; f++) a.qs[f] = h->mixed ? (const T *)qin32[f] : (const T *)qin.f[f];
@@ -852,6 +866,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.sigma = h->sigma;
     a.savg = h->savg;
     for (int d = 0; d < 3; d++) {
+        a.threads = h->threads[d];
         a.L = h->L[d];
         a.lgL = ilog2(h->L[d]);
         a.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));

@@ -2,16 +2,24 @@
 #pragma once
 #include "cs3d_dev.cuh"
 
-#ifndef CS3D_TPB
-#define CS3D_TPB 256  // threads per block of the mixed-form stage sweeps
+#ifndef CS3D_TPB_X
+#define CS3D_TPB_X 256   // threads per block of the mixed-form x sweep
+#endif
+#ifndef CS3D_TPB_YZ
+#define CS3D_TPB_YZ 512  // most threads per block of the mixed-form y and z sweeps
 #endif
 
 namespace cs3d {
 
-// threads per block of the stage sweeps in work type T (the plain FP64 form
-// needs up to 255 registers per thread and runs 128)
+// Most threads per block the stage sweeps in work type T, direction dir, are
+// compiled for.  The mixed-form x sweep (80 registers) runs 3 blocks of 256
+// per SM; the y and z sweeps (up to 128 registers) run either 2 blocks of 256
+// or one block of 512 on a tile twice as wide (the host picks per direction).
+// The plain FP64 form needs up to 255 registers per thread and runs 128.
 template <typename T>
-__host__ __device__ constexpr int sweep_threads() { return sizeof(T) == 4 ? CS3D_TPB : 128; }
+__host__ __device__ constexpr int sweep_threads(int dir) {
+    return sizeof(T) == 4 ? (dir == 0 ? CS3D_TPB_X : CS3D_TPB_YZ) : 128;
+}
 
 #ifndef CS3D_FTPB
 #define CS3D_FTPB 256  // threads per block of the mixed-form filter

@@ -44,20 +44,37 @@
 #ifndef CS3D_ZC2
 #define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
 #endif
-// Resident blocks per SM the mixed-form sweeps are compiled for (256 threads
-// each: x at 3 blocks / 80 registers, y and z at 2 blocks / 128 registers
-// were fastest at 128^3); the plain form runs 128 threads, 2 blocks.
+// Resident blocks per SM the mixed-form sweeps are compiled for: x at 3
+// blocks of 256 threads (80 registers), y and z at one block of 512 (128
+// registers); the plain form runs 128 threads, 2 blocks.
 #ifndef CS3D_MINB_X
 #define CS3D_MINB_X 3
 #endif
 #ifndef CS3D_MINB_Y
-#define CS3D_MINB_Y 2
+#define CS3D_MINB_Y 1
 #endif
 #ifndef CS3D_MINB_Z
-#define CS3D_MINB_Z 2
+#define CS3D_MINB_Z 1
 #endif
 
 namespace cs3d {
+
+// The y and z sweeps' solves (D1 and D2, H = 2).  In the mixed form at
+// buffer pitch 8 the pitch is a compile-time constant, so that a chunk's
+// shared-memory accesses are immediates off one base register (measured 3%
+// faster); at pitch 16, and in the x sweep (pitch L + 1) and the filter, the
+// extra instantiation measured slower than the run-time pitch.
+template <typename T>
+__device__ __forceinline__ void run_solves(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
+                                           const LineOp<T> &d1, const LineOp<T> &d2) {
+    if constexpr (sizeof(T) == 4) {
+        if (sm.P == 8) {
+            run_tasks<T, 2, 8>(sm, tasks, ntask, L, nlines, d1, d2);
+            return;
+        }
+    }
+    run_tasks<T, 2>(sm, tasks, ntask, L, nlines, d1, d2);
+}
 
 // ---------------------------------------------------------------------
 // sweep x
@@ -68,7 +85,7 @@ __constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}
                                 {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -160,7 +177,7 @@ __constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}
                                 {YF4, YF4, 0, YF4, YF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -195,7 +212,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
             sm.b(YF4)[o] = re * V + V * pp;
         });
     __syncthreads();
-    run_tasks<T, 2>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
+    run_solves<T>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
@@ -246,7 +263,7 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
 template <typename T>
-__global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
     const int L = a.L, P = a.P;
     const Tile t = make_tile<2>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -284,7 +301,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
             sm.b(ZF4)[o] = re * W + W * pp;
         });
     __syncthreads();
-    run_tasks<T, 2>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
+    run_solves<T>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), c23 = T(2.0 / 3.0), cpPr = (T)a.gas.cpPr;
     const double dt = *a.dt;
@@ -466,7 +483,6 @@ __global__ void __launch_bounds__(sweep_threads<T>(), sizeof(T) == 4 ? CS3D_MINB
 // middle pass works in FP32, and the last pass writes
 // q1 = q2 + (filtered - unfiltered) in FP64 plus q1's FP32 shadow.
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
-__constant__ Task kTasksFc[3] = {{0, 5, 2, 1, 6, 2}, {2, 7, 2, 3, 8, 2}, {4, 9, 2, 4, 9, 2}};
 
 template <typename T, int DIR>
 __global__ void __launch_bounds__(filter_threads<T>()) k_filter(FilterArgs<T> a) {
@@ -495,7 +511,18 @@ __global__ void __launch_bounds__(filter_threads<T>()) k_filter(FilterArgs<T> a)
         }
     }
     __syncthreads();
-    run_tasks<T, 4>(sm, kCorr ? kTasksFc : kTasksF, 3, L, t.nlines, a.op, a.op);
+    if constexpr (kCorr) {
+        // the five right-hand sides by the whole block, then one thread per
+        // (field, line) for the recurrences alone
+        rhs_pass<T, 4, 5>(sm, 0, 5, L, a.lgL, t.nlines, a.op);
+        __syncthreads();
+        for (int w = threadIdx.x; w < 5 * L; w += blockDim.x) {
+            const int l = w & (L - 1), f = w >> a.lgL;
+            if (l < t.nlines) thomas_inplace<T, 4>(sm.b(5 + f) + l, a.op, &sm.fact[(5 + f) * L + l], P);
+        }
+    } else {
+        run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
+    }
     __syncthreads();
     for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
         Pt pt[B];

@@ -40,10 +40,13 @@ __device__ __forceinline__ void boundary_rows(const T *src, int P, const LineOp<
 // (1st and 2nd derivative of one field: A in place, B into its own buffer).
 // The Sherman-Morrison factor of a periodic line is formed in FP64 from the
 // line's end values and stored to f* in the work precision.
-template <typename T, int H>
+template <typename T, int H, int PC = 0>
 __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &oa, T *fa, const T *sb, T *db,
-                                           const LineOp<T> &ob, T *fb, int P) {
+                                           const LineOp<T> &ob, T *fb, int P_) {
     constexpr int W = 2 * H + 1;
+    // PC > 0: the buffer pitch as a compile-time constant, so that every
+    // shared-memory access of a chunk is a base register plus an immediate
+    const int P = PC > 0 ? PC : P_;
     const int N = oa.N;
     T pa[2 * H], pb[2 * H];
     boundary_rows<T, H>(sa, P, oa, pa);
@@ -206,6 +209,99 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     *fb = ob.periodic ? (T)((to_f64(xb) + ob.bog * to_f64(xlb)) * ob.inv_den) : T(0);
 }
 
+// Row n of the explicit right-hand side of a line read from src (stride P):
+// the interior stencil, or the explicit boundary row (wrapped columns), with
+// the products summed in the same order as solve_pair.
+template <typename T, int H>
+__device__ __forceinline__ T rhs_row(const T *src, int P, const LineOp<T> &op, int n) {
+    const int N = op.N;
+    T acc = T(0);
+    if (n >= H && n < N - H) {
+#pragma unroll
+        for (int k = 0; k < 2 * H + 1; ++k) acc = fma(op.taps[kMaxH - H + k], src[(n - H + k) * P], acc);
+        return acc;
+    }
+    const int b = n < H ? n : n - (N - H) + H;
+    const int col = op.boff[b];
+#pragma unroll
+    for (int k = 0; k < kTaps; ++k) {
+        int cc = col + k;
+        cc = cc < 0 ? cc + N : (cc >= N ? cc - N : cc);
+        acc = fma(op.btaps[b][k], src[cc * P], acc);
+    }
+    return acc;
+}
+
+// One Thomas solve in place on a line whose right-hand side is already in d
+// (stride P): forward and backward recurrences in chunks of kU rows with the
+// next chunk's values and 128-bit coefficient loads issued ahead (reads past
+// the line's end land in the buffer's padding rows and the coefficient
+// arrays' zero padding).  Same operations in the same order as solve_pair.
+template <typename T, int H>
+__device__ __forceinline__ void thomas_inplace(T *d, const LineOp<T> &op, T *fac, int P) {
+    const int N = op.N;
+    T y = d[0];
+#pragma unroll
+    for (int n = 1; n < H; ++n) {
+        y = fma(-__ldg(&op.m[n]), y, d[n * P]);
+        d[n * P] = y;
+    }
+    const int nend = N - H;
+    int n = H;
+    T rn[kU], mn[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) rn[j] = d[(n + j) * P];
+    load4(op.mf, mn);
+#pragma unroll 2
+    for (; n + kU <= nend; n += kU) {
+        T rc[kU], mc[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) { rc[j] = rn[j]; mc[j] = mn[j]; }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) rn[j] = d[(n + kU + j) * P];
+        load4(op.mf + (n + kU - H), mn);
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            y = fma(-mc[j], y, rc[j]);
+            d[(n + j) * P] = y;
+        }
+    }
+    for (; n < N; ++n) {
+        y = fma(-__ldg(&op.m[n]), y, d[n * P]);
+        d[n * P] = y;
+    }
+    T x = y * __ldg(&op.iw[N - 1]);
+    d[(N - 1) * P] = x;
+    const T xl = x;
+    n = N - 2;
+    T y4[kU], c4[kU], i4[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) y4[j] = d[max(n - j, 0) * P];
+    load4(op.cbk, c4);
+    load4(op.ibk, i4);
+#pragma unroll 2
+    for (; n - kU + 1 >= 0; n -= kU) {
+        T y0[kU], c0[kU], i0[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) { y0[j] = y4[j]; c0[j] = c4[j]; i0[j] = i4[j]; }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) y4[j] = d[max(n - kU - j, 0) * P];
+        const int kb = N - 2 - (n - kU);
+        load4(op.cbk + kb, c4);
+        load4(op.ibk + kb, i4);
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            x = fma(-c0[j], x, y0[j]) * i0[j];
+            d[(n - j) * P] = x;
+        }
+    }
+    for (; n >= 0; --n) {
+        x = fma(-__ldg(&op.c[n]), x, d[n * P]) * __ldg(&op.iw[n]);
+        d[n * P] = x;
+    }
+    *fac = op.periodic ? (T)((to_f64(x) + op.bog * to_f64(xl)) * op.inv_den) : T(0);
+}
+
 // Corrected value of solution n of a line whose factor is f.
 template <typename T>
 __device__ __forceinline__ T corr(T x, T f, const LineOp<T> &op, int n) {
@@ -322,6 +418,40 @@ __device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
     return s;
 }
 
+// Right-hand sides of nf line solves per line, computed by every thread of
+// the block: buffer dst0 + f gets the right-hand side of buffer src0 + f.
+// A work item is 4 consecutive rows of one (field, line); interior items
+// slide a register window over the 4 + 2H rows they need.  Lines are the
+// fastest index, so a warp reads consecutive banks.
+template <typename T, int H, int NF>
+__device__ __forceinline__ void rhs_pass(const Smem<T> &sm, int src0, int dst0, int L, int lgL, int nlines,
+                                         const LineOp<T> &op) {
+    constexpr int R = 4;
+    const int N = op.N, P = sm.P;
+    const int ng = (N + R - 1) / R;
+    for (int w = threadIdx.x; w < NF * ng * L; w += blockDim.x) {
+        const int l = w & (L - 1), g = w >> lgL;
+        if (l >= nlines) continue;
+        const int f = g % NF, n0 = (g / NF) * R;
+        const T *src = sm.b(src0 + f) + l;
+        T *dst = sm.b(dst0 + f) + l;
+        if (n0 >= H && n0 + R <= N - H) {
+            T e[R + 2 * H];
+#pragma unroll
+            for (int k = 0; k < R + 2 * H; ++k) e[k] = src[(n0 - H + k) * P];
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                T acc = T(0);
+#pragma unroll
+                for (int k = 0; k < 2 * H + 1; ++k) acc = fma(op.taps[kMaxH - H + k], e[j + k], acc);
+                dst[(n0 + j) * P] = acc;
+            }
+        } else {
+            for (int n = n0; n < min(n0 + R, N); ++n) dst[n * P] = rhs_row<T, H>(src, P, op, n);
+        }
+    }
+}
+
 // Per-thread loop over the points of a tile with a software pipeline: the
 // global loads of the thread's next point are issued before the current
 // point is computed, so memory latency overlaps the arithmetic.
@@ -368,7 +498,8 @@ struct Task {
     signed char a, da, oa, b, db, ob;
 };
 
-template <typename T, int H>
+// PC > 0: the caller has checked that the buffer pitch sm.P equals PC.
+template <typename T, int H, int PC = 0>
 __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
                                           const LineOp<T> &op0, const LineOp<T> &op1) {
     for (int w = threadIdx.x; w < ntask * L; w += blockDim.x) {
@@ -377,8 +508,8 @@ __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, 
         const Task tk = tasks[t];
         const LineOp<T> &oa = tk.oa == 1 ? op1 : op0;
         const LineOp<T> &ob = tk.ob == 1 ? op1 : op0;
-        solve_pair<T, H>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
-                         sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
+        solve_pair<T, H, PC>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
+                             sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
     }
 }
 
