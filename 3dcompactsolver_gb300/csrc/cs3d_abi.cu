@@ -258,6 +258,22 @@ int upload_op(const HostOp &h, DevOp<T> &d, cudaStream_t s) {
         o.boff[b] = h.boff[b];
     }
     o.scale = (T)h.scale;
+    // the run of rows around the middle with bitwise constant factors in T
+    o.klo = o.khi = 1;
+    if (N >= 8) {
+        const int mid = N / 2;
+        auto same = [&](int i) {
+            return (T)h.m[i] == (T)h.m[mid] && (T)h.iw[i] == (T)h.iw[mid] && (T)h.c[i] == (T)h.c[mid];
+        };
+        int lo = mid, hi = mid + 1;
+        while (lo > 1 && same(lo - 1)) --lo;
+        while (hi < N - 1 && same(hi)) ++hi;
+        o.klo = lo;
+        o.khi = hi;
+    }
+    o.km = (T)h.m[N / 2];
+    o.kiw = (T)h.iw[N / 2];
+    o.kc = (T)h.c[N / 2];
     o.bog = h.bog;
     o.inv_den = h.inv_den;
     o.N = N;

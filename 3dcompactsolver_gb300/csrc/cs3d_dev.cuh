@@ -33,6 +33,11 @@ struct LineOp {
     T btaps[2 * kMaxH][kTaps]; // the first H and last H rows, explicit
     int boff[2 * kMaxH]; // first column of each boundary row
     T scale;             // 1/h, 1/h^2 or 1
+    // Rows [klo, khi) (1 <= klo <= khi <= N-1) where m, iw and c equal km,
+    // kiw, kc bit for bit in T: the factors of the Toeplitz interior converge
+    // geometrically, and there the recurrences run on register constants.
+    T km, kiw, kc;
+    int klo, khi;
     double bog;          // beta / gamma of the cyclic correction
     double inv_den;      // 1 / (1 + z_0 + beta z_{N-1} / gamma)
     int N;
@@ -40,16 +45,51 @@ struct LineOp {
     int periodic;
 };
 
-// Four consecutive elements from a 16-byte aligned address in one or two
-// 128-bit loads (read-only path).
+// Loads of operator coefficients (a few kB per operator, read by every line
+// solve): read-only path with L1 evict-last priority, so that the tiles'
+// streaming loads do not push them out of L1.
+#ifndef CS3D_COEF_EVICT_LAST
+#define CS3D_COEF_EVICT_LAST 1
+#endif
+__device__ __forceinline__ float ldc(const float *p) {
+#if CS3D_COEF_EVICT_LAST
+    float v;
+    asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+__device__ __forceinline__ double ldc(const double *p) {
+#if CS3D_COEF_EVICT_LAST
+    double v;
+    asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+
+// Four consecutive coefficients from a 16-byte aligned address in one or two
+// 128-bit loads.
 __device__ __forceinline__ void load4(const float *p, float v[4]) {
+#if CS3D_COEF_EVICT_LAST
+    asm("ld.global.nc.L1::evict_last.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "l"(p));
+#else
     const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
     v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+#endif
 }
 __device__ __forceinline__ void load4(const double *p, double v[4]) {
+#if CS3D_COEF_EVICT_LAST
+    asm("ld.global.nc.L1::evict_last.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "l"(p));
+    asm("ld.global.nc.L1::evict_last.v2.f64 {%0, %1}, [%2];" : "=d"(v[2]), "=d"(v[3]) : "l"(p + 2));
+#else
     const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
     const double2 b = __ldg(reinterpret_cast<const double2 *>(p + 2));
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+#endif
 }
 
 // Conserved variables of one state (five FP64 arrays, XYZ layout).

@@ -485,7 +485,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
 
 template <typename T, int DIR>
-__global__ void __launch_bounds__(filter_threads<T>()) k_filter(FilterArgs<T> a) {
+__global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? 3 : 4) k_filter(FilterArgs<T> a) {
     constexpr int B = sizeof(T) == 4 ? CS3D_FB : 2;
     constexpr bool kCorr = sizeof(T) == 4;
     const int L = a.L, P = a.P;
@@ -518,7 +518,11 @@ __global__ void __launch_bounds__(filter_threads<T>()) k_filter(FilterArgs<T> a)
         __syncthreads();
         for (int w = threadIdx.x; w < 5 * L; w += blockDim.x) {
             const int l = w & (L - 1), f = w >> a.lgL;
-            if (l < t.nlines) thomas_inplace<T, 4>(sm.b(5 + f) + l, a.op, &sm.fact[(5 + f) * L + l], P);
+            if (l >= t.nlines) continue;
+            T *d = sm.b(5 + f) + l, *fc = &sm.fact[(5 + f) * L + l];
+            if (P == 8) thomas_inplace<T, 8>(d, a.op, fc, 8);
+            else if (P == 9) thomas_inplace<T, 9>(d, a.op, fc, 9);
+            else thomas_inplace<T, 0>(d, a.op, fc, P);
         }
     } else {
         run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
@@ -599,7 +603,7 @@ static size_t tile_smem(int nbuf, int L, int P, int N) {
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
     return prec_bytes == 8 ? tile_smem<double>(nbuf, L, P, N) : tile_smem<float>(nbuf, L, P, N);
 }
-int sweep_nbuf(int dir) { return dir == 0 ? XNB : dir == 1 ? YNB : ZNB; }
+int sweep_nbuf(int dir) { return dir == 0 ? (int)XNB : dir == 1 ? (int)YNB : (int)ZNB; }
 int sweep_ntask(int dir) { return dir == 0 ? 7 : 8; }
 int filter_ntask() { return 3; }
 

@@ -4,6 +4,7 @@
 #pragma once
 #include "cs3d_dev.cuh"
 #include "cs3d_kernels.cuh"
+#include <type_traits>
 
 namespace cs3d {
 
@@ -72,14 +73,20 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     db[0] = yb;
 #pragma unroll
     for (int n = 1; n < H; ++n) {
-        ya = fma(-__ldg(&ma[n]), ya, pa[n]);
-        yb = fma(-__ldg(&mb[n]), yb, pb[n]);
+        ya = fma(-ldc(&ma[n]), ya, pa[n]);
+        yb = fma(-ldc(&mb[n]), yb, pb[n]);
         da[n * P] = ya;
         db[n * P] = yb;
     }
-    // interior rows H..N-H-1 in chunks of kU, next chunk prefetched
+    // interior rows H..N-H-1 in chunks of kU, next chunk prefetched.  Chunks
+    // inside [klo, khi) of both operators (chunk starts kept on the kU
+    // lattice from H, so the 128-bit factor loads stay aligned) run on the
+    // register constants km; the others load m through mf.
     const int nend = N - H;
     int n = H;
+    const int klo = max(oa.klo, ob.klo), khi = min(oa.khi, ob.khi);
+    const int clo = H + kU * ((max(klo - H, 0) + kU - 1) / kU);
+    const T kma = oa.km, kmb = ob.km;
     T na[kU], nb[kU], mna[kU], mnb[kU];
 #pragma unroll
     for (int j = 0; j < kU; ++j) {
@@ -89,12 +96,14 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     }
     load4(oa.mf, mna);
     load4(ob.mf, mnb);
-#pragma unroll 2
-    for (; n + kU <= nend; n += kU) {
+    auto fwd_chunk = [&](auto kconst) {
+        constexpr bool K = decltype(kconst)::value;
         T ca[kU], cb[kU], mca[kU], mcb[kU];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
-            ca[j] = na[j]; cb[j] = nb[j]; mca[j] = mna[j]; mcb[j] = mnb[j];
+            ca[j] = na[j]; cb[j] = nb[j];
+            mca[j] = K ? kma : mna[j];
+            mcb[j] = K ? kmb : mnb[j];
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
@@ -102,8 +111,10 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
             na[j] = sa[pos * P];
             nb[j] = sb[pos * P];
         }
-        load4(oa.mf + (n + kU - H), mna);
-        load4(ob.mf + (n + kU - H), mnb);
+        if (!K) {
+            load4(oa.mf + (n + kU - H), mna);
+            load4(ob.mf + (n + kU - H), mnb);
+        }
         T ea[W + kU], eb[W + kU];
 #pragma unroll
         for (int k = 0; k < W; ++k) { ea[k] = wa[k]; eb[k] = wb[k]; }
@@ -130,7 +141,20 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
         }
 #pragma unroll
         for (int k = 0; k < W; ++k) { wa[k] = ea[kU + k]; wb[k] = eb[kU + k]; }
+    };
+    // (the plain FP64 form keeps one loop: the constants' registers would
+    // cost it a resident block per SM, and its time is FP64 arithmetic)
+    if constexpr (sizeof(T) == 4) {
+        for (; n + kU <= nend && n < clo; n += kU) fwd_chunk(std::false_type{});
+        if (n + kU <= khi) {
+#pragma unroll 2
+            for (; n + kU <= nend && n + kU <= khi; n += kU) fwd_chunk(std::true_type{});
+            load4(oa.mf + (n - H), mna);
+            load4(ob.mf + (n - H), mnb);
+        }
     }
+#pragma unroll 2
+    for (; n + kU <= nend; n += kU) fwd_chunk(std::false_type{});
     for (; n < nend; ++n) {
         T acc_a = T(0), acc_b = T(0);
 #pragma unroll
@@ -138,8 +162,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
             acc_a = fma(ta[k], wa[k], acc_a);
             acc_b = fma(tb[k], wb[k], acc_b);
         }
-        ya = fma(-__ldg(&ma[n]), ya, acc_a);
-        yb = fma(-__ldg(&mb[n]), yb, acc_b);
+        ya = fma(-ldc(&ma[n]), ya, acc_a);
+        yb = fma(-ldc(&mb[n]), yb, acc_b);
 #pragma unroll
         for (int k = 0; k < W - 1; ++k) { wa[k] = wa[k + 1]; wb[k] = wb[k + 1]; }
         const int pos = n + H + 1;
@@ -152,8 +176,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
 #pragma unroll
     for (int b = 0; b < H; ++b) {
         const int r = N - H + b;
-        ya = fma(-__ldg(&ma[r]), ya, pa[H + b]);
-        yb = fma(-__ldg(&mb[r]), yb, pb[H + b]);
+        ya = fma(-ldc(&ma[r]), ya, pa[H + b]);
+        yb = fma(-ldc(&mb[r]), yb, pb[H + b]);
         da[r * P] = ya;
         db[r * P] = yb;
     }
@@ -162,8 +186,8 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     const T *__restrict__ cb_ = ob.c;
     const T *__restrict__ ia = oa.iw;
     const T *__restrict__ ib = ob.iw;
-    T xa = ya * __ldg(&ia[N - 1]);
-    T xb = yb * __ldg(&ib[N - 1]);
+    T xa = ya * ldc(&ia[N - 1]);
+    T xb = yb * ldc(&ib[N - 1]);
     da[(N - 1) * P] = xa;
     db[(N - 1) * P] = xb;
     const T xla = xa, xlb = xb;
@@ -176,21 +200,30 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     }
     load4(oa.cbk, cA); load4(ob.cbk, cB);
     load4(oa.ibk, iA); load4(ob.ibk, iB);
-#pragma unroll 2
-    for (; n - kU + 1 >= 0; n -= kU) {
+    // chunk tops on the lattice N-2-kU*k; chunks wholly inside [klo, khi)
+    // run on the constants kc, kiw
+    const T kca = oa.kc, kcb = ob.kc, kia = oa.kiw, kib = ob.kiw;
+    auto bwd_chunk = [&](auto kconst) {
+        constexpr bool K = decltype(kconst)::value;
         T y0a[kU], y0b[kU], c0a[kU], c0b[kU], i0a[kU], i0b[kU];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
-            y0a[j] = ya4[j]; y0b[j] = yb4[j]; c0a[j] = cA[j]; c0b[j] = cB[j]; i0a[j] = iA[j]; i0b[j] = iB[j];
+            y0a[j] = ya4[j]; y0b[j] = yb4[j];
+            c0a[j] = K ? kca : cA[j];
+            c0b[j] = K ? kcb : cB[j];
+            i0a[j] = K ? kia : iA[j];
+            i0b[j] = K ? kib : iB[j];
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
             const int r = max(n - kU - j, 0);
             ya4[j] = da[r * P]; yb4[j] = db[r * P];
         }
-        const int kb = N - 2 - (n - kU);
-        load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
-        load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+        if (!K) {
+            const int kb = N - 2 - (n - kU);
+            load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+            load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+        }
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
             xa = fma(-c0a[j], xa, y0a[j]) * i0a[j];
@@ -198,10 +231,22 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
             da[(n - j) * P] = xa;
             db[(n - j) * P] = xb;
         }
+    };
+    if constexpr (sizeof(T) == 4) {
+        for (; n - kU + 1 >= 0 && n >= khi; n -= kU) bwd_chunk(std::false_type{});
+        if (n - kU + 1 >= klo) {
+#pragma unroll 2
+            for (; n - kU + 1 >= klo; n -= kU) bwd_chunk(std::true_type{});
+            const int kb = N - 2 - n;
+            load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+            load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+        }
     }
+#pragma unroll 2
+    for (; n - kU + 1 >= 0; n -= kU) bwd_chunk(std::false_type{});
     for (; n >= 0; --n) {
-        xa = fma(-__ldg(&ca_[n]), xa, da[n * P]) * __ldg(&ia[n]);
-        xb = fma(-__ldg(&cb_[n]), xb, db[n * P]) * __ldg(&ib[n]);
+        xa = fma(-ldc(&ca_[n]), xa, da[n * P]) * ldc(&ia[n]);
+        xb = fma(-ldc(&cb_[n]), xb, db[n * P]) * ldc(&ib[n]);
         da[n * P] = xa;
         db[n * P] = xb;
     }
@@ -233,70 +278,86 @@ __device__ __forceinline__ T rhs_row(const T *src, int P, const LineOp<T> &op, i
 }
 
 // One Thomas solve in place on a line whose right-hand side is already in d
-// (stride P): forward and backward recurrences in chunks of kU rows with the
-// next chunk's values and 128-bit coefficient loads issued ahead (reads past
-// the line's end land in the buffer's padding rows and the coefficient
-// arrays' zero padding).  Same operations in the same order as solve_pair.
-template <typename T, int H>
-__device__ __forceinline__ void thomas_inplace(T *d, const LineOp<T> &op, T *fac, int P) {
-    const int N = op.N;
+// (stride P, a compile-time constant when PC > 0).  Rows outside [klo, khi)
+// load their factors; rows inside run on the register constants km, kiw, kc
+// in chunks of kU with the next chunk's values read ahead (reads past the
+// body stay inside the line).  The operations and their order are those of
+// solve_pair, so the results are the same bit for bit.
+template <typename T, int PC>
+__device__ __forceinline__ void thomas_inplace(T *d, const LineOp<T> &op, T *fac, int P_) {
+    const int P = PC > 0 ? PC : P_;
+    const int N = op.N, lo = op.klo, hi = op.khi;
+    const T km = op.km, kiw = op.kiw, kc = op.kc;
+    // forward: y_0 = r_0, y_n = r_n - m_n y_{n-1}
     T y = d[0];
-#pragma unroll
-    for (int n = 1; n < H; ++n) {
-        y = fma(-__ldg(&op.m[n]), y, d[n * P]);
+    int n = 1;
+    for (; n < lo; ++n) {
+        y = fma(-ldc(&op.m[n]), y, d[n * P]);
         d[n * P] = y;
     }
-    const int nend = N - H;
-    int n = H;
-    T rn[kU], mn[kU];
+    if (n + kU <= hi) {
+        T rn[kU];
 #pragma unroll
-    for (int j = 0; j < kU; ++j) rn[j] = d[(n + j) * P];
-    load4(op.mf, mn);
+        for (int j = 0; j < kU; ++j) rn[j] = d[(n + j) * P];
 #pragma unroll 2
-    for (; n + kU <= nend; n += kU) {
-        T rc[kU], mc[kU];
+        for (; n + kU <= hi; n += kU) {
+            T rc[kU];
 #pragma unroll
-        for (int j = 0; j < kU; ++j) { rc[j] = rn[j]; mc[j] = mn[j]; }
+            for (int j = 0; j < kU; ++j) rc[j] = rn[j];
+            if (n + 2 * kU <= hi) {
 #pragma unroll
-        for (int j = 0; j < kU; ++j) rn[j] = d[(n + kU + j) * P];
-        load4(op.mf + (n + kU - H), mn);
+                for (int j = 0; j < kU; ++j) rn[j] = d[(n + kU + j) * P];
+            }
 #pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            y = fma(-mc[j], y, rc[j]);
-            d[(n + j) * P] = y;
+            for (int j = 0; j < kU; ++j) {
+                y = fma(-km, y, rc[j]);
+                d[(n + j) * P] = y;
+            }
         }
     }
-    for (; n < N; ++n) {
-        y = fma(-__ldg(&op.m[n]), y, d[n * P]);
+    for (; n < hi; ++n) {
+        y = fma(-km, y, d[n * P]);
         d[n * P] = y;
     }
-    T x = y * __ldg(&op.iw[N - 1]);
+    for (; n < N; ++n) {
+        y = fma(-ldc(&op.m[n]), y, d[n * P]);
+        d[n * P] = y;
+    }
+    // backward: x_{N-1} = y_{N-1} iw_{N-1}, x_n = (y_n - c_n x_{n+1}) iw_n
+    T x = y * ldc(&op.iw[N - 1]);
     d[(N - 1) * P] = x;
     const T xl = x;
     n = N - 2;
-    T y4[kU], c4[kU], i4[kU];
+    for (; n >= hi; --n) {
+        x = fma(-ldc(&op.c[n]), x, d[n * P]) * ldc(&op.iw[n]);
+        d[n * P] = x;
+    }
+    if (n - kU + 1 >= lo) {
+        T y4[kU];
 #pragma unroll
-    for (int j = 0; j < kU; ++j) y4[j] = d[max(n - j, 0) * P];
-    load4(op.cbk, c4);
-    load4(op.ibk, i4);
+        for (int j = 0; j < kU; ++j) y4[j] = d[(n - j) * P];
 #pragma unroll 2
-    for (; n - kU + 1 >= 0; n -= kU) {
-        T y0[kU], c0[kU], i0[kU];
+        for (; n - kU + 1 >= lo; n -= kU) {
+            T y0[kU];
 #pragma unroll
-        for (int j = 0; j < kU; ++j) { y0[j] = y4[j]; c0[j] = c4[j]; i0[j] = i4[j]; }
+            for (int j = 0; j < kU; ++j) y0[j] = y4[j];
+            if (n - 2 * kU + 1 >= lo) {
 #pragma unroll
-        for (int j = 0; j < kU; ++j) y4[j] = d[max(n - kU - j, 0) * P];
-        const int kb = N - 2 - (n - kU);
-        load4(op.cbk + kb, c4);
-        load4(op.ibk + kb, i4);
+                for (int j = 0; j < kU; ++j) y4[j] = d[(n - kU - j) * P];
+            }
 #pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            x = fma(-c0[j], x, y0[j]) * i0[j];
-            d[(n - j) * P] = x;
+            for (int j = 0; j < kU; ++j) {
+                x = fma(-kc, x, y0[j]) * kiw;
+                d[(n - j) * P] = x;
+            }
         }
     }
+    for (; n >= lo; --n) {
+        x = fma(-kc, x, d[n * P]) * kiw;
+        d[n * P] = x;
+    }
     for (; n >= 0; --n) {
-        x = fma(-__ldg(&op.c[n]), x, d[n * P]) * __ldg(&op.iw[n]);
+        x = fma(-ldc(&op.c[n]), x, d[n * P]) * ldc(&op.iw[n]);
         d[n * P] = x;
     }
     *fac = op.periodic ? (T)((to_f64(x) + op.bog * to_f64(xl)) * op.inv_den) : T(0);
@@ -305,7 +366,7 @@ __device__ __forceinline__ void thomas_inplace(T *d, const LineOp<T> &op, T *fac
 // Corrected value of solution n of a line whose factor is f.
 template <typename T>
 __device__ __forceinline__ T corr(T x, T f, const LineOp<T> &op, int n) {
-    return op.periodic ? fma(-f, __ldg(&op.z[n]), x) : x;
+    return op.periodic ? fma(-f, ldc(&op.z[n]), x) : x;
 }
 
 // ---------------------------------------------------------------------
@@ -527,8 +588,8 @@ struct Zn {
 template <typename T>
 __device__ __forceinline__ Zn<T> zn(const LineOp<T> &d1, const LineOp<T> &d2, int n) {
     Zn<T> z;
-    z.z1 = d1.periodic ? __ldg(&d1.z[n]) : T(0);
-    z.z2 = d2.periodic ? __ldg(&d2.z[n]) : T(0);
+    z.z1 = d1.periodic ? ldc(&d1.z[n]) : T(0);
+    z.z2 = d2.periodic ? ldc(&d2.z[n]) : T(0);
     return z;
 }
 // Corrected solution of buffer k at point p, with z the operator's vector.
