@@ -38,6 +38,9 @@
 #ifndef CS3D_FB
 #define CS3D_FB 4      // points per thread in flight in the mixed filter's load and store loops
 #endif
+#ifndef CS3D_FMINB
+#define CS3D_FMINB 3   // resident blocks per SM the mixed filter is compiled for
+#endif
 #ifndef CS3D_ZC1
 #define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
 #endif
@@ -59,23 +62,11 @@
 
 namespace cs3d {
 
-// The y and z sweeps' solves (D1 and D2, H = 2).  In the mixed form at
-// buffer pitch 8 the pitch is a compile-time constant, so that a chunk's
-// shared-memory accesses are immediates off one base register (measured 3%
-// faster); at pitch 16, and in the x sweep (pitch L + 1) and the filter, the
-// extra instantiation measured slower than the run-time pitch.
-template <typename T>
-__device__ __forceinline__ void run_solves(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
-                                           const LineOp<T> &d1, const LineOp<T> &d2) {
-    if constexpr (sizeof(T) == 4) {
-        if (sm.P == 8) {
-            run_tasks<T, 2, 8>(sm, tasks, ntask, L, nlines, d1, d2);
-            return;
-        }
-    }
-    run_tasks<T, 2>(sm, tasks, ntask, L, nlines, d1, d2);
-}
-
+// The sweep kernels take the shared-memory pitch of their tile as a template
+// parameter PC (0: read at run time).  The launcher instantiates the mixed
+// form's usual pitches (x: 9 and 5; y, z: 16 and 8), where every
+// shared-memory access of a solve chunk becomes an immediate off one base
+// register: x 0.358 -> 0.336 ms, y and z 2-4% faster per step at 128^3.
 // ---------------------------------------------------------------------
 // sweep x
 // ---------------------------------------------------------------------
@@ -84,9 +75,9 @@ __constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}
                                 {XT, XT, 0, XT, XT2, 1}, {XRU, XRU, 0, XF1, XF1, 0},
                                 {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XF4, 0}};
 
-template <typename T>
+template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
-    const int L = a.L, P = a.P;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(XNB, L, P, N);
@@ -130,7 +121,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
             sm.b(XF4)[o] = s.re * ss.U + ss.U * ss.p;
         });
     __syncthreads();
-    run_tasks<T, 2>(sm, kTasksX, 7, L, t.nlines, a.d1, a.d2);
+    run_tasks<T, 2, PC>(sm, kTasksX, 7, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     // phase C
     const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
@@ -176,9 +167,9 @@ __constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}
                                 {YRV, YRV, 0, YF1, YF1, 0}, {YF2, YF2, 0, YF3, YF3, 0},
                                 {YF4, YF4, 0, YF4, YF4, 0}};
 
-template <typename T>
+template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
-    const int L = a.L, P = a.P;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(YNB, L, P, N);
@@ -212,7 +203,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
             sm.b(YF4)[o] = re * V + V * pp;
         });
     __syncthreads();
-    run_solves<T>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
+    run_tasks<T, 2, PC>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
@@ -262,9 +253,9 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZWY, ZWY, 0, ZRW, ZRW, 0}, {ZF1, ZF1, 0, ZF2, ZF2, 0},
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
-template <typename T>
+template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
-    const int L = a.L, P = a.P;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<2>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(ZNB, L, P, N);
@@ -301,7 +292,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
             sm.b(ZF4)[o] = re * W + W * pp;
         });
     __syncthreads();
-    run_solves<T>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
+    run_tasks<T, 2, PC>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), c23 = T(2.0 / 3.0), cpPr = (T)a.gas.cpPr;
     const double dt = *a.dt;
@@ -485,7 +476,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
 
 template <typename T, int DIR>
-__global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? 3 : 4) k_filter(FilterArgs<T> a) {
+__global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMINB : 4) k_filter(FilterArgs<T> a) {
     constexpr int B = sizeof(T) == 4 ? CS3D_FB : 2;
     constexpr bool kCorr = sizeof(T) == 4;
     const int L = a.L, P = a.P;
@@ -626,9 +617,17 @@ cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s) {
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
     const size_t sm = tile_smem<T>(sweep_nbuf(dir), a.L, a.P, N);
     const dim3 grid = tile_grid(dir, a.g, a.L);
-    if (dir == 0) return launch_tile_kernel(k_sweep_x<T>, a, grid, sm, s);
-    if (dir == 1) return launch_tile_kernel(k_sweep_y<T>, a, grid, sm, s);
-    return launch_tile_kernel(k_sweep_z<T>, a, grid, sm, s);
+    if constexpr (sizeof(T) == 4) {
+        if (dir == 0 && a.P == 9) return launch_tile_kernel(k_sweep_x<T, 9>, a, grid, sm, s);
+        if (dir == 0 && a.P == 5) return launch_tile_kernel(k_sweep_x<T, 5>, a, grid, sm, s);
+        if (dir == 1 && a.P == 16) return launch_tile_kernel(k_sweep_y<T, 16>, a, grid, sm, s);
+        if (dir == 1 && a.P == 8) return launch_tile_kernel(k_sweep_y<T, 8>, a, grid, sm, s);
+        if (dir == 2 && a.P == 16) return launch_tile_kernel(k_sweep_z<T, 16>, a, grid, sm, s);
+        if (dir == 2 && a.P == 8) return launch_tile_kernel(k_sweep_z<T, 8>, a, grid, sm, s);
+    }
+    if (dir == 0) return launch_tile_kernel(k_sweep_x<T, 0>, a, grid, sm, s);
+    if (dir == 1) return launch_tile_kernel(k_sweep_y<T, 0>, a, grid, sm, s);
+    return launch_tile_kernel(k_sweep_z<T, 0>, a, grid, sm, s);
 }
 
 template <typename T>
