@@ -467,6 +467,8 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
 // ---------------------------------------------------------------------
 // compact filter, one direction, five fields (Filter.cpp:98-171)
 // ---------------------------------------------------------------------
+// PC: the tile pitch as a compile-time constant (0: at run time); the mixed
+// form's 128^3 pitches (x 9, y and z 8) are instantiated.
 // Plain form: FP64 in, FP64 out, a.op = F.  Mixed form: a.op is the
 // correction F - I, solved out of place (buffers 5..9), and the pass writes
 // v + (F - I) v; the first pass reads FP64 q2 minus a per-field reference
@@ -475,11 +477,11 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
 // q1 = q2 + (filtered - unfiltered) in FP64 plus q1's FP32 shadow.
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
 
-template <typename T, int DIR>
+template <typename T, int DIR, int PC>
 __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMINB : 4) k_filter(FilterArgs<T> a) {
     constexpr int B = sizeof(T) == 4 ? CS3D_FB : 2;
     constexpr bool kCorr = sizeof(T) == 4;
-    const int L = a.L, P = a.P;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<DIR>(a.g, L);
     const int N = t.N, NL = N * L;
     Smem<T> sm = smem_layout<T>(kCorr ? 10 : 5, L, P, N);
@@ -510,10 +512,7 @@ __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMI
         for (int w = threadIdx.x; w < 5 * L; w += blockDim.x) {
             const int l = w & (L - 1), f = w >> a.lgL;
             if (l >= t.nlines) continue;
-            T *d = sm.b(5 + f) + l, *fc = &sm.fact[(5 + f) * L + l];
-            if (P == 8) thomas_inplace<T, 8>(d, a.op, fc, 8);
-            else if (P == 9) thomas_inplace<T, 9>(d, a.op, fc, 9);
-            else thomas_inplace<T, 0>(d, a.op, fc, P);
+            thomas_inplace<T, PC>(sm.b(5 + f) + l, a.op, &sm.fact[(5 + f) * L + l], P);
         }
     } else {
         run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
@@ -635,9 +634,14 @@ cudaError_t launch_filter(int dir, const FilterArgs<T> &a, cudaStream_t s) {
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
     const size_t sm = tile_smem<T>(sizeof(T) == 4 ? 10 : 5, a.L, a.P, N);
     const dim3 grid = tile_grid(dir, a.g, a.L);
-    if (dir == 0) return launch_tile_kernel(k_filter<T, 0>, a, grid, sm, s);
-    if (dir == 1) return launch_tile_kernel(k_filter<T, 1>, a, grid, sm, s);
-    return launch_tile_kernel(k_filter<T, 2>, a, grid, sm, s);
+    if constexpr (sizeof(T) == 4) {
+        if (dir == 0 && a.P == 9) return launch_tile_kernel(k_filter<T, 0, 9>, a, grid, sm, s);
+        if (dir == 1 && a.P == 8) return launch_tile_kernel(k_filter<T, 1, 8>, a, grid, sm, s);
+        if (dir == 2 && a.P == 8) return launch_tile_kernel(k_filter<T, 2, 8>, a, grid, sm, s);
+    }
+    if (dir == 0) return launch_tile_kernel(k_filter<T, 0, 0>, a, grid, sm, s);
+    if (dir == 1) return launch_tile_kernel(k_filter<T, 1, 0>, a, grid, sm, s);
+    return launch_tile_kernel(k_filter<T, 2, 0>, a, grid, sm, s);
 }
 
 cudaError_t launch_line_op(const LineOpArgs &a, cudaStream_t s) {
