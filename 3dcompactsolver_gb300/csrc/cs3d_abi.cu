@@ -317,6 +317,8 @@ struct cs3d_handle {
     Q5 q1{}, qk{}, q2{};
     float *q1s[5] = {}, *qks[5] = {}, *q2s[5] = {};
     int mixed_rk4 = 0;  // mixed form with RK4: the stage input qk lives in qks only
+    float *racc[5] = {};  // mixed RK4: FP32 sum of b_i dq_i over stages 1-3
+    int acc_live = 0;     // stages 1-3 of a step are done: q2 = q1 + racc
     double *dq[5] = {};
     // work-precision fields (double or float, by tb)
     void *prim[5] = {}, *mu = nullptr, *amu = nullptr, *dx4[4] = {}, *dy4[4] = {}, *R[5] = {}, *diag[3] = {};
@@ -596,6 +598,7 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             ALLOC(h->q1s[f], n * 4);
             ALLOC(h->qks[f], n * 4);
             ALLOC(h->q2s[f], n * 4);
+            if (h->mixed_rk4) ALLOC(h->racc[f], n * 4);
         }
     }
     ALLOC(h->mu, n * h->tb);
@@ -760,6 +763,7 @@ extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, c
 // maximum for the first step.
 static int init_after_state(cs3d_handle *h) {
     const size_t n = (size_t)h->g.npts;
+    h->acc_live = 0;
     if (h->sponge)
         for (int f = 0; f < 5; f++)
             CS3D_CUDA(cudaMemcpyAsync(h->savg.f[f], h->q1.f[f], n * 8, cudaMemcpyDeviceToDevice, h->stream));
@@ -870,6 +874,8 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.q2 = h->q2;
     a.qk = h->qk;
     a.mixed_rk4 = h->mixed_rk4;
+    for (int f = 0; f < 5; f++) a.acc[f] = h->racc[f];
+    h->acc_live = h->mixed_rk4 && !last;
     // FP32 shadow written by the z sweep: the next stage's input, or -- after
     // the last stage of a step that is not filtered -- q2, which becomes q1
     a.shadow_target = SHADOW_NONE;
@@ -1033,7 +1039,20 @@ static int field_ptr(cs3d_handle *h, int field, double **p) {
             h->launches++;
         }
     }
-    else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) *p = h->q2.f[field - CS3D_F_RHO2];
+    else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) {
+        *p = h->q2.f[field - CS3D_F_RHO2];
+        if (h->acc_live) {
+            // mid-step in the mixed RK4 form: the accumulator is q1 + acc
+            ShadowArgs a{};
+            a.g = h->g;
+            a.q.f[0] = *p;
+            a.in[0] = h->racc[field - CS3D_F_RHO2];
+            a.base[0] = h->q1.f[field - CS3D_F_RHO2];
+            a.nf = 1;
+            CS3D_CUDA(launch_shadow(a, h->stream));
+            h->launches++;
+        }
+    }
     else if (field >= CS3D_F_RHOK2 && field < CS3D_F_RHOK2 + 5) {
         if (!h->store_dq) return fail(CS3D_ERR_STATE, "increments are kept only with CS3D_OPT_STORE_INCREMENTS");
         *p = h->dq[field - CS3D_F_RHOK2];

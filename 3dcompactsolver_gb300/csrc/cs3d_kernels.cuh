@@ -67,6 +67,7 @@ struct SweepArgs {
     int rk, rk_step;
     Q5 q1, q2, qk;
     const float *q1s[5];    // FP32 shadow of q1 (mixed RK4, stages 2-3)
+    float *acc[5];          // mixed RK4: FP32 sum of b_i dq_i over stages 1-3
     float *shadow_out[5];   // FP32 shadow of the next stage input (mixed)
     int shadow_target;      // ShadowTarget
     int mixed_rk4;          // mixed form with RK4: qk kept only as FP32 shadow
@@ -162,6 +163,7 @@ struct ShadowArgs {
     Q5 q;
     float *out[5];
     const float *in[5];
+    const double *base[5];  // with in: q = base + in (FP64), else q = in
     int nf;
 };
 

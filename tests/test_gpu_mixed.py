@@ -77,3 +77,28 @@ def test_mixed_tracks_fp64(gpu_pkg, cases, name):
         assert np.isfinite(a).all()
         d = np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
         assert d < 1e-4, (name, f, d)
+
+
+def test_mixed_rk4_accumulator_mid_step(gpu_pkg, cases):
+    """The mixed RK4 form sums the stage increments b_i dq_i in FP32 and adds
+    them to q1 on the last stage; read between stages, the RK accumulator q2
+    (fields 10..14) is q1 + sum b_i dq_i as in RK4.hpp:35-118."""
+    cfg, ic = cases.tgv(16, precision=gpu_pkg.FP32_MIXED)
+    s = gpu_pkg.Solver(cfg)
+    s.set_initial_conditions(*ic)
+    s.run(2)
+    s.set_option(gpu_pkg.OPT_STORE_INCREMENTS, 1)
+    q1 = s.conserved()
+    s.pre_step()
+    acc = np.zeros_like(q1)
+    for st, b in ((1, 1 / 6), (2, 1 / 3), (3, 1 / 3)):
+        s.sub_step(st, 0)
+        dq = np.stack([s.get(15 + f) for f in range(5)])
+        acc += b * dq
+        q2 = np.stack([s.get(10 + f) for f in range(5)])
+        for f in range(5):
+            # FP32 rounding of the partial sums of the increments
+            tol = 1e-6 * np.abs(acc[f]).max() + 1e-15 * np.abs(q1[f]).max()
+            assert np.abs(q2[f] - (q1[f] + acc[f])).max() <= tol, (st, f)
+    s.sub_step(4, 1)
+    s.close()
