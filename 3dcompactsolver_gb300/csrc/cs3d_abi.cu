@@ -874,7 +874,11 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.q2 = h->q2;
     a.qk = h->qk;
     a.mixed_rk4 = h->mixed_rk4;
-    for (int f = 0; f < 5; f++) a.acc[f] = h->racc[f];
+    for (int f = 0; f < 5; f++) {
+        a.acc[f] = h->racc[f];
+        a.fref[f] = h->fref[f];
+    }
+    a.fluct_out = h->mixed_rk4 && last && filtered;
     h->acc_live = h->mixed_rk4 && !last;
     // FP32 shadow written by the z sweep: the next stage's input, or -- after
     // the last stage of a step that is not filtered -- q2, which becomes q1
@@ -928,11 +932,15 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                 void **dst = pass == 0 ? h->ft1 : h->ft2;
                 for (int f = 0; f < 5; f++) {
                     fa.ref[f] = h->mixed ? h->fref[f] : 0.0;
-                    fa.src64.f[f] = pass == 0 ? h->q2.f[f] : nullptr;
-                    fa.src32[f] = pass == 0 ? nullptr : (T *)src[f];
+                    // first pass: q2 - fref, in FP32 from the last stage (mixed
+                    // RK4) or formed here from FP64 q2
+                    const bool fl = pass == 0 && h->mixed_rk4;
+                    fa.src64.f[f] = pass == 0 && !fl ? h->q2.f[f] : nullptr;
+                    fa.src32[f] = fl ? (T *)h->racc[f] : pass == 0 ? nullptr : (T *)src[f];
                     fa.dst64.f[f] = pass == 2 ? h->q1.f[f] : nullptr;
                     fa.dst32[f] = pass == 2 ? nullptr : (T *)dst[f];
                     fa.delta_from.f[f] = (pass == 2 && h->mixed) ? h->q2.f[f] : nullptr;
+                    fa.unf[f] = (pass == 2 && h->mixed_rk4) ? h->racc[f] : nullptr;
                     fa.shadow_out[f] = (pass == 2 && h->mixed) ? h->q1s[f] : nullptr;
                 }
                 tstart(h, CS3D_K_FILTER);
@@ -1840,6 +1848,7 @@ extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double
         CS3D_CUDA(cudaMemcpyAsync(grad_host + (size_t)f * n, QB[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
     // back to the recorded final state
     if ((rc = adj_set_state(h, FIN))) return rc;
+    h->acc_live = 0;
     h->timeStep = h->adj_end_ts;
     h->filterTimeStep = h->adj_end_fts;
     CS3D_CUDA(cudaMemcpyAsync(h->scal, h->adj_end_scal, 2 * 8, cudaMemcpyHostToDevice, h->stream));

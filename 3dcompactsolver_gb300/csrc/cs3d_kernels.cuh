@@ -68,6 +68,8 @@ struct SweepArgs {
     Q5 q1, q2, qk;
     const float *q1s[5];    // FP32 shadow of q1 (mixed RK4, stages 2-3)
     float *acc[5];          // mixed RK4: FP32 sum of b_i dq_i over stages 1-3
+    int fluct_out;          // mixed RK4, last stage of a filtered step: acc <- q2 - fref (FP32)
+    double fref[5];         // the filter's per-field reference values
     float *shadow_out[5];   // FP32 shadow of the next stage input (mixed)
     int shadow_target;      // ShadowTarget
     int mixed_rk4;          // mixed form with RK4: qk kept only as FP32 shadow
@@ -88,6 +90,7 @@ struct FilterArgs {
     Q5 dst64;          // FP64 destination (or null pointers)
     T *dst32[5];       // work-precision destination
     Q5 delta_from;     // mixed last pass: q1 = q2 + (filtered - unfiltered)
+    const float *unf[5];   // mixed last pass: the unfiltered first-pass input, if kept
     float *shadow_out[5];  // mixed last pass: FP32 shadow of q1
     double ref[5];     // per-field reference value subtracted on entry
 };

@@ -120,19 +120,34 @@ __global__ void k_cfl(CflArgs a) {
     double mx = 0.0;
     int bad = 0;
     if (a.qs[0]) {
+        // FP32 shadow: four consecutive points per thread (128-bit loads of
+        // the 16-byte aligned arrays), one reciprocal of rho per point
         float fm = 0.f;
         const float gam = (float)a.gas.gamma, gm1 = (float)a.gas.gm1;
         const float idx = a.idx, idy = a.idy, idz = a.idz;
-        for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
-             gi += (long long)gridDim.x * blockDim.x) {
-            const float r = a.qs[0][gi];
-            const float U = a.qs[1][gi] / r, V = a.qs[2][gi] / r, W = a.qs[3][gi] / r;
-            const float p = gm1 * (a.qs[4][gi] - 0.5f * r * (U * U + V * V + W * W));
-            const float c = sqrtf(gam * p / r);
+        auto point = [&](float r, float ru, float rv, float rw, float re) {
+            const float ir = 1.0f / r;
+            const float U = ru * ir, V = rv * ir, W = rw * ir;
+            const float p = gm1 * (re - 0.5f * r * (U * U + V * V + W * W));
+            const float c = sqrtf(gam * p * ir);
             const float v = (fabsf(U) + c) * idx + (fabsf(V) + c) * idy + (fabsf(W) + c) * idz;
             bad |= !(v == v) || isinf(v);
             fm = fmaxf(fm, v);
+        };
+        const long long n4 = a.g.npts >> 2;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+             i += (long long)gridDim.x * blockDim.x) {
+            float4 q[5];
+#pragma unroll
+            for (int f = 0; f < 5; ++f) q[f] = __ldg(reinterpret_cast<const float4 *>(a.qs[f]) + i);
+            point(q[0].x, q[1].x, q[2].x, q[3].x, q[4].x);
+            point(q[0].y, q[1].y, q[2].y, q[3].y, q[4].y);
+            point(q[0].z, q[1].z, q[2].z, q[3].z, q[4].z);
+            point(q[0].w, q[1].w, q[2].w, q[3].w, q[4].w);
         }
+        for (long long gi = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
+             gi += (long long)gridDim.x * blockDim.x)
+            point(a.qs[0][gi], a.qs[1][gi], a.qs[2][gi], a.qs[3][gi], a.qs[4][gi]);
         mx = widen(fm);
     } else {
         for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;

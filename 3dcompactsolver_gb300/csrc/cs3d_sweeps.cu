@@ -38,6 +38,9 @@
 #ifndef CS3D_FB
 #define CS3D_FB 4      // points per thread in flight in the mixed filter's load and store loops
 #endif
+#ifndef CS3D_FBC
+#define CS3D_FBC 2     // points per thread in flight in the mixed filter's consume loop
+#endif
 #ifndef CS3D_FMINB
 #define CS3D_FMINB 3   // resident blocks per SM the mixed filter is compiled for
 #endif
@@ -462,6 +465,8 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
                             const double q2n = in.qa[f] + to_f64(fma(ca, d, (T)in.acc[f]));
                             a.q2.f[f][gi] = q2n;
                             if (a.shadow_target == SHADOW_Q2) a.shadow_out[f][gi] = narrow(q2n);
+                            // the filter's first pass input, q2 - fref in FP32
+                            if (a.fluct_out) a.acc[f][gi] = narrow(q2n - a.fref[f]);
                         }
                     }
                 }
@@ -523,17 +528,22 @@ __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMI
         run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
     }
     __syncthreads();
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
-        Pt pt[B];
-        double q[B][5];
+    constexpr int BC = sizeof(T) == 4 ? CS3D_FBC : 2;
+    for (int p0 = threadIdx.x; p0 < NL; p0 += BC * blockDim.x) {
+        Pt pt[BC];
+        double q[BC][5];
+        T u[BC][5];
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
+        for (int b = 0; b < BC; ++b) {
             pt[b] = point<DIR>(t, p0 + b * blockDim.x, L, P, a.lgL, a.divN);
 #pragma unroll
-            for (int f = 0; f < 5; ++f) q[b][f] = a.delta_from.f[f] ? a.delta_from.f[f][pt[b].gi] : 0.0;
+            for (int f = 0; f < 5; ++f) {
+                q[b][f] = a.delta_from.f[f] ? a.delta_from.f[f][pt[b].gi] : 0.0;
+                u[b][f] = kCorr && a.unf[f] ? (T)a.unf[f][pt[b].gi] : T(0);
+            }
         }
 #pragma unroll
-        for (int b = 0; b < B; ++b) {
+        for (int b = 0; b < BC; ++b) {
             if (!pt[b].ok) continue;
             const unsigned gi = pt[b].gi;
 #pragma unroll
@@ -542,7 +552,9 @@ __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMI
                 if (a.dst64.f[f]) {
                     double nv;
                     if (a.delta_from.f[f]) {
-                        const T v0 = to_work<T>(q[b][f] - a.ref[f]);
+                        // the unfiltered value: the first pass's FP32 input, or
+                        // formed again from q2 (the same number either way)
+                        const T v0 = kCorr && a.unf[f] ? u[b][f] : to_work<T>(q[b][f] - a.ref[f]);
                         nv = q[b][f] + to_f64(v - v0);
                     } else {
                         nv = to_f64(v) + a.ref[f];
