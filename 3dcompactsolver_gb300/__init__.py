@@ -67,6 +67,8 @@ def lib():
         L.cs3d_get_field.argtypes = [_H, ctypes.c_int, _DP]
         L.cs3d_set_field.argtypes = [_H, ctypes.c_int, _DP]
         L.cs3d_field_ptr.argtypes = [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        L.cs3d_get_conserved.argtypes = [_H, ctypes.POINTER(_DP)]
+        L.cs3d_set_conserved.argtypes = [_H, ctypes.POINTER(_DP)]
         L.cs3d_get_scalars.argtypes = [_H, _DP, _DP, ctypes.POINTER(ctypes.c_int)]
         L.cs3d_get_stream.argtypes = [_H, ctypes.POINTER(ctypes.c_void_p)]
         L.cs3d_launch_count.argtypes = [_H, ctypes.POINTER(ctypes.c_longlong)]
@@ -165,7 +167,16 @@ class Solver:
 
     def conserved(self):
         """q1 as a (5, Nz, Ny, Nx) array."""
-        return np.stack([self.get(_abi.F_RHO1 + f) for f in range(5)])
+        out = np.empty((5,) + tuple(self.shape), np.float64)
+        ptrs = (_DP * 5)(*[_dptr(out[f]) for f in range(5)])
+        check(lib().cs3d_get_conserved(self.h, ptrs))
+        return out
+
+    def set_conserved(self, q):
+        """Set q1 from a (5, Nz, Ny, Nx) array (all five fields, one call)."""
+        a = [np.ascontiguousarray(q[f], dtype=np.float64) for f in range(5)]
+        ptrs = (_DP * 5)(*[_dptr(x) for x in a])
+        check(lib().cs3d_set_conserved(self.h, ptrs))
 
     def scalars(self):
         dt, t, ts = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()

@@ -1122,6 +1122,42 @@ extern "C" int cs3d_set_field(cs3d_handle *h, int field, const double *host_in) 
     return CS3D_OK;
 }
 
+extern "C" int cs3d_get_conserved(cs3d_handle *h, double *const host_out[5]) {
+    if (!h || !host_out) return fail(CS3D_ERR_ARG, "null argument");
+    for (int f = 0; f < 5; f++)
+        if (!host_out[f]) return fail(CS3D_ERR_ARG, "null field %d", f);
+    DeviceGuard dg(h->dev);
+    const size_t bytes = (size_t)h->g.npts * 8;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(host_out[f], h->q1.f[f], bytes, cudaMemcpyDeviceToHost, h->stream));
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_set_conserved(cs3d_handle *h, const double *const host_in[5]) {
+    if (!h || !host_in) return fail(CS3D_ERR_ARG, "null argument");
+    for (int f = 0; f < 5; f++)
+        if (!host_in[f]) return fail(CS3D_ERR_ARG, "null field %d", f);
+    DeviceGuard dg(h->dev);
+    const size_t bytes = (size_t)h->g.npts * 8;
+    for (int f = 0; f < 5; f++)
+        CS3D_CUDA(cudaMemcpyAsync(h->q1.f[f], host_in[f], bytes, cudaMemcpyHostToDevice, h->stream));
+    if (h->mixed) {
+        // the FP32 shadow of q1, all five fields in one launch
+        ShadowArgs a{};
+        a.g = h->g;
+        for (int f = 0; f < 5; f++) {
+            a.q.f[f] = h->q1.f[f];
+            a.out[f] = h->q1s[f];
+        }
+        a.nf = 5;
+        CS3D_CUDA(launch_shadow(a, h->stream));
+        h->launches++;
+    }
+    CS3D_CUDA(cudaStreamSynchronize(h->stream));
+    return CS3D_OK;
+}
+
 extern "C" int cs3d_field_ptr(cs3d_handle *h, int field, double **dev_ptr) {
     if (!h || !dev_ptr) return fail(CS3D_ERR_ARG, "null argument");
     DeviceGuard dg(h->dev);

@@ -41,23 +41,38 @@ UNIT = "Mpts/s per RK stage"
 # work arrays 4 bytes in the mixed form, 8 in the plain form); see the
 # kernel byte model in the design doc.
 def kernel_bytes_per_point(kernel, wb, rk_stages):
-    if kernel == "sweep_x":
-        return 40 + wb * (5 + 2 + 4 + 5)              # q* in; prims, mu, mu', 4 derivs, 5 RHS out
-    if kernel == "sweep_y":
-        return 32 + wb * (5 + 2 + 1 + 5) + wb * (4 + 5)  # q*(4), prims, Ux Vx, mu, RHS in; 4 derivs, RHS out
-    if kernel == "sweep_z":
-        common = 40 + wb * (5 + 4 + 4 + 2 + 5)        # q*, prims, x/y derivs, mu mu', RHS
-        if rk_stages == 4:   # RK4: st1 writes q2,qk; st2-3 read q1,q2 write q2,qk; st4 reads q1,q2 writes q2
-            per = [common + 80, common + 80 + 80, common + 80 + 80, common + 80 + 40]
-        else:                # TVD-RK3: st1 writes qk; st2 reads q1 writes qk; st3 reads q1 writes q2
-            per = [common + 40, common + 40 + 40, common + 40 + 40]
+    """Algorithmic bytes per grid point of one launch: every array the kernel
+    reads or writes, counted once (no walls or sponge).  wb = 4 is the mixed
+    form (FP32 work arrays, FP32 shadow of the stage input, FP64 state), 8 the
+    plain FP64 form."""
+    mixed = wb == 4
+    if kernel == "sweep_x":    # q* in; prims, mu, mu', Ux..Tx, R out
+        return wb * 5 + wb * (5 + 2 + 4 + 5)
+    if kernel == "sweep_y":    # q*(4), prims, Ux Vx, mu, R in; Uy..Ty, R out
+        return wb * (4 + 5 + 2 + 1 + 5) + wb * (4 + 5)
+    if kernel == "sweep_z":    # q*, prims, Ux..Tx, Uy..Ty, mu mu', R in, then the RK update
+        common = wb * (5 + 5 + 4 + 4 + 2 + 5)
+        if rk_stages == 4 and mixed:
+            # st1: qk, acc out; st2-3: acc, q1 shadow in, qk, acc out;
+            # st4: q1, acc in, q2 out, and q2 - fref for the filter (filtered steps)
+            per = [common + 40, common + 40 + 40, common + 40 + 40, common + 60 + 40 + 20]
+        elif rk_stages == 4:
+            # st1: q1 in, q2 qk out; st2-3: q1 q2 in, q2 qk out; st4: q2 in, q2 out
+            per = [common + 40 + 80, common + 80 + 80, common + 80 + 80, common + 40 + 40]
+        else:
+            # TVD-RK3: st1: q1 in, qk out; st2: q1 qk in, qk out; st3: q1 qk in, q2 out
+            # (the mixed form adds the FP32 shadow it writes)
+            sh = 20 if mixed else 0
+            per = [common + 40 + 40 + sh, common + 80 + 40 + sh, common + 80 + 40 + sh]
         return sum(per) / len(per)
     if kernel == "filter":
-        if wb == 8:
-            return 80.0                                # 5 fields in, 5 out, FP64
-        return (40 + 20 + 20 + 20 + 20 + 40 + 40) / 3.0  # mixed: q2 in, FP32 passes, q2 + q1 last
+        if not mixed:
+            return 80.0        # 5 FP64 fields in, 5 out
+        # FP32 in/out on the first two passes; the last reads the FP32 field,
+        # the first pass's input and FP64 q2, and writes FP64 q1 and its shadow
+        return (40 + 40 + (20 + 20 + 40 + 40 + 20)) / 3.0
     if kernel == "cfl":
-        return 40.0
+        return 20.0 if mixed else 40.0
     return 0.0
 
 
@@ -342,16 +357,14 @@ def run_ours(args):
     for f in range(5):
         q_host[f].numpy()[...] = s.get(f)
     lib = pkg.lib()
-    ptrs = [q.numpy().ctypes.data_as(pkg._DP) for q in q_host]
+    ptrs = (pkg._DP * 5)(*[q.numpy().ctypes.data_as(pkg._DP) for q in q_host])
     torch.cuda.synchronize()
     _barrier(ws)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for f in range(5):
-            pkg.check(lib.cs3d_set_field(s.h, f, ptrs[f]))
+        pkg.check(lib.cs3d_set_conserved(s.h, ptrs))
         pkg.check(lib.cs3d_step(s.h))
-        for f in range(5):
-            pkg.check(lib.cs3d_get_field(s.h, f, ptrs[f]))
+        pkg.check(lib.cs3d_get_conserved(s.h, ptrs))
     e2e_s = _barrier_max(time.perf_counter() - t0, ws)
     e2e_val = ws * npts * stages * args.steps / e2e_s / 1e6
 

@@ -145,6 +145,12 @@ int cs3d_sync(cs3d_handle *h);
 /* Copy a field (Nx*Ny*Nz doubles, XYZ layout) between host and device. */
 int cs3d_get_field(cs3d_handle *h, int field, double *host_out);
 int cs3d_set_field(cs3d_handle *h, int field, const double *host_in);
+/* The conserved state q1 (rho1, rhoU1, rhoV1, rhoW1, rhoE1; AbstractCSolver.hpp:
+ * 19-26) between host and device in one call: the five copies are queued
+ * together and waited for once.  Same result as cs3d_get_field /
+ * cs3d_set_field on fields 0..4. */
+int cs3d_get_conserved(cs3d_handle *h, double *const host_out[5]);
+int cs3d_set_conserved(cs3d_handle *h, const double *const host_in[5]);
 /* Device pointer of a field (XYZ layout, FP64), valid until destroy. */
 int cs3d_field_ptr(cs3d_handle *h, int field, double **dev_ptr);
 
