@@ -643,6 +643,12 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             h->threads[d] = sweep_threads<float>(d);
         }
         h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB");
+        // a mixed filter tile narrower than 8 lines within 72 kB (N = 256: 4
+        // lines, 16-byte rows) takes the widest within 110 kB instead (2
+        // blocks per SM): HIT 256^3 filter 2.27 -> 1.81 ms per step; at
+        // N = 128 the 8-line tile stays (16 lines measured slower)
+        if (h->mixed && h->Lf[d] < 8 && !getenv("CS3D_FILTER_SMEM_KB"))
+            h->Lf[d] = pick_L(h->tb, 10, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB", 110);
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
