@@ -47,6 +47,9 @@
 #ifndef CS3D_ZC1
 #define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
 #endif
+#ifndef CS3D_YC
+#define CS3D_YC 4      // points per thread in flight in the y sweep's consume phase
+#endif
 #ifndef CS3D_ZC2
 #define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
 #endif
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
-    batched<InC, 2>(NL,
+    batched<InC, sizeof(T) == 4 ? CS3D_YC : 2>(NL,
         [&](InC &in, int p) {
             in.pt = point<1>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
