@@ -3,8 +3,8 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload tgv128|tgv64|hit256|shear] [--precision mixed|fp64]
 
-Prints ONE JSON line on rank 0.  The metric is the benchmark's: million grid
-points advanced per second per Runge-Kutta stage ("Mpts/s per RK stage"),
+Prints ONE JSON line on rank 0.  The metric: million grid points advanced
+per second per Runge-Kutta stage ("Mpts/s per RK stage"),
 i.e. npts * stages * steps / seconds.  A "step" is one full time step of the
 solver (4 RK4 stages or 3 TVD-RK3 stages, the filter and the CFL reduction).
 
@@ -38,8 +38,7 @@ UNIT = "Mpts/s per RK stage"
 
 # Algorithmic bytes per grid point of each kernel launch, for the roofline.
 # Counted from the arrays each kernel must read and write once (state FP64;
-# work arrays 4 bytes in the mixed form, 8 in the plain form); see the
-# kernel byte model in the design doc.
+# work arrays 4 bytes in the mixed form, 8 in the plain form).
 def kernel_bytes_per_point(kernel, wb, rk_stages):
     """Algorithmic bytes per grid point of one launch: every array the kernel
     reads or writes, counted once (no walls or sponge).  wb = 4 is the mixed
