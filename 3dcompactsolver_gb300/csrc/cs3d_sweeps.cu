@@ -42,7 +42,7 @@
 #define CS3D_FBC 2     // points per thread in flight in the mixed filter's consume loop
 #endif
 #ifndef CS3D_FMINB
-#define CS3D_FMINB 3   // resident blocks per SM the mixed filter is compiled for
+#define CS3D_FMINB 4   // resident blocks per SM the mixed filter is compiled for (64 registers)
 #endif
 #ifndef CS3D_ZC1
 #define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
