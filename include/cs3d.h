@@ -91,7 +91,11 @@ typedef struct cs3d_config {
 #define CS3D_F_RHOW1  3
 #define CS3D_F_RHOE1  4
 #define CS3D_F_RHOK   5   /* rhok..rhoEk: stage input (qk)      5..9  */
-#define CS3D_F_RHO2   10  /* rho2..rhoE2: RK accumulator (q2)  10..14 */
+#define CS3D_F_RHO2   10  /* rho2..rhoE2: RK accumulator (q2)  10..14;
+                             between the stages of an FP32-mixed RK4 step the
+                             accumulator is q1 plus an FP32 sum of the stage
+                             increments: reads form that sum, writes there do
+                             not reach the step's last stage */
 #define CS3D_F_RHOK2  15  /* rhok2..rhoEk2: last increment dq  15..19 */
 #define CS3D_F_U      20  /* U V W p T mu sos from q1 (the solver's
                              primitives after the last stage)  20..26 */
