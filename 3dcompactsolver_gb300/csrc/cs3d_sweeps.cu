@@ -50,6 +50,9 @@
 #ifndef CS3D_YC
 #define CS3D_YC 4      // points per thread in flight in the y sweep's consume phase
 #endif
+#ifndef CS3D_ZC1_PIPE
+#define CS3D_ZC1_PIPE 1  // the z sweep's right-hand-side pass software-pipelined (0: batched)
+#endif
 #ifndef CS3D_ZC2
 #define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
 #endif
@@ -328,7 +331,11 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
         T v[18];
         T qsv[5];
     };
+#if CS3D_ZC1_PIPE
+    pipelined<InC1>(NL,
+#else
     batched<InC1, CS3D_ZC1>(NL,
+#endif
         [&](InC1 &in, int p) {
             in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
