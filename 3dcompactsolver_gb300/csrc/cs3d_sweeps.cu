@@ -45,7 +45,7 @@
 #define CS3D_FMINB 4   // resident blocks per SM the mixed filter is compiled for (64 registers)
 #endif
 #ifndef CS3D_ZC1
-#define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass
+#define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass (batched form)
 #endif
 #ifndef CS3D_YC
 #define CS3D_YC 4      // points per thread in flight in the y sweep's consume phase
