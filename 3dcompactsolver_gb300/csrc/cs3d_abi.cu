@@ -317,8 +317,7 @@ struct cs3d_handle {
     Q5 q1{}, qk{}, q2{};
     float *q1s[5] = {}, *qks[5] = {}, *q2s[5] = {};
     int mixed_rk4 = 0;  // mixed form with RK4: the stage input qk lives in qks only
-    float *racc[5] = {};  // mixed RK4: FP32 sum of b_i dq_i over stages 1-3
-    int acc_live = 0;     // stages 1-3 of a step are done: q2 = q1 + racc
+    float *rfluct[5] = {};  // mixed RK4: q2 - fref in FP32 after a filtered step's last stage
     double *dq[5] = {};
     // work-precision fields (double or float, by tb)
     void *prim[5] = {}, *mu = nullptr, *amu = nullptr, *dx4[4] = {}, *dy4[4] = {}, *R[5] = {}, *diag[3] = {};
@@ -493,17 +492,12 @@ static int check_config(const cs3d_config *c) {
 }
 
 // Tile width: the widest power of two (<= 32 lines) whose shared memory
-// stays within the per-block budget of 72 KB, three blocks per SM.  For the
+// stays within a per-block budget (72 kB: three blocks per SM).  For the
 // y and z sweeps of the mixed form at N = 128 this gives 8 lines: every
 // global access is then a full 32-byte sector, which measured faster than
-// narrower tiles with more blocks per SM.  CS3D_SMEM_BUDGET_KB overrides it.
-static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, const char *env = "CS3D_SMEM_BUDGET_KB",
-                  int budget_kb = 72) {
-    size_t budget = (size_t)budget_kb * 1024;
-    if (const char *e = getenv(env)) {
-        long v = strtol(e, nullptr, 10);
-        if (v >= 8 && v <= 220) budget = (size_t)v * 1024;
-    }
+// narrower tiles with more blocks per SM.
+static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, int budget_kb = 72) {
+    const size_t budget = (size_t)budget_kb * 1024;
     int L = 32;
     while (L > 1 && sweep_smem_bytes((int)tb, nbuf, L, L + pitch_plus, N) > budget) L /= 2;
     return L;
@@ -598,7 +592,7 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             ALLOC(h->q1s[f], n * 4);
             ALLOC(h->qks[f], n * 4);
             ALLOC(h->q2s[f], n * 4);
-            if (h->mixed_rk4) ALLOC(h->racc[f], n * 4);
+            if (h->mixed_rk4) ALLOC(h->rfluct[f], n * 4);
         }
     }
     ALLOC(h->mu, n * h->tb);
@@ -638,26 +632,18 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         // slower, its phases no longer overlapping another block's.
         h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
         h->threads[d] = h->mixed ? (d == 0 ? sweep_threads<float>(0) : 256) : sweep_threads<double>(d);
-        if (h->mixed && d > 0 && h->L[d] < 16 && !getenv("CS3D_SMEM_BUDGET_KB")) {
-            h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], 0, "CS3D_SMEM_BUDGET_KB", 200);
+        if (h->mixed && d > 0 && h->L[d] < 16) {
+            h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], 0, 200);
             h->threads[d] = sweep_threads<float>(d);
         }
-        h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB");
+        h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0);
         // a mixed filter tile narrower than 8 lines within 72 kB (N = 256: 4
         // lines, 16-byte rows) takes the widest within 110 kB instead (2
         // blocks per SM): HIT 256^3 filter 2.27 -> 1.81 ms per step; at
         // N = 128 the 8-line tile stays (16 lines measured slower)
-        if (h->mixed && h->Lf[d] < 8 && !getenv("CS3D_FILTER_SMEM_KB"))
-            h->Lf[d] = pick_L(h->tb, 10, Nd[d], d == 0 ? 1 : 0, "CS3D_FILTER_SMEM_KB", 110);
+        if (h->mixed && h->Lf[d] < 8) h->Lf[d] = pick_L(h->tb, 10, Nd[d], d == 0 ? 1 : 0, 110);
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
-    }
-    if (const char *e = getenv("CS3D_THREADS")) {
-        long v = strtol(e, nullptr, 10);
-        for (int d = 0; d < 3; d++) {
-            const int mx = h->mixed ? sweep_threads<float>(d) : sweep_threads<double>(d);
-            if (v > 0 && v <= mx && v % 32 == 0) h->threads[d] = (int)v;
-        }
     }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
@@ -769,7 +755,6 @@ extern "C" int cs3d_set_initial_conditions(cs3d_handle *h, const double *rho0, c
 // maximum for the first step.
 static int init_after_state(cs3d_handle *h) {
     const size_t n = (size_t)h->g.npts;
-    h->acc_live = 0;
     if (h->sponge)
         for (int f = 0; f < 5; f++)
             CS3D_CUDA(cudaMemcpyAsync(h->savg.f[f], h->q1.f[f], n * 8, cudaMemcpyDeviceToDevice, h->stream));
@@ -881,11 +866,10 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.qk = h->qk;
     a.mixed_rk4 = h->mixed_rk4;
     for (int f = 0; f < 5; f++) {
-        a.acc[f] = h->racc[f];
+        a.fluct[f] = h->rfluct[f];
         a.fref[f] = h->fref[f];
     }
     a.fluct_out = h->mixed_rk4 && last && filtered;
-    h->acc_live = h->mixed_rk4 && !last;
     // FP32 shadow written by the z sweep: the next stage's input, or -- after
     // the last stage of a step that is not filtered -- q2, which becomes q1
     a.shadow_target = SHADOW_NONE;
@@ -942,11 +926,11 @@ static int run_stage(cs3d_handle *h, int st, int last) {
                     // RK4) or formed here from FP64 q2
                     const bool fl = pass == 0 && h->mixed_rk4;
                     fa.src64.f[f] = pass == 0 && !fl ? h->q2.f[f] : nullptr;
-                    fa.src32[f] = fl ? (T *)h->racc[f] : pass == 0 ? nullptr : (T *)src[f];
+                    fa.src32[f] = fl ? (T *)h->rfluct[f] : pass == 0 ? nullptr : (T *)src[f];
                     fa.dst64.f[f] = pass == 2 ? h->q1.f[f] : nullptr;
                     fa.dst32[f] = pass == 2 ? nullptr : (T *)dst[f];
                     fa.delta_from.f[f] = (pass == 2 && h->mixed) ? h->q2.f[f] : nullptr;
-                    fa.unf[f] = (pass == 2 && h->mixed_rk4) ? h->racc[f] : nullptr;
+                    fa.unf[f] = (pass == 2 && h->mixed_rk4) ? h->rfluct[f] : nullptr;
                     fa.shadow_out[f] = (pass == 2 && h->mixed) ? h->q1s[f] : nullptr;
                 }
                 tstart(h, CS3D_K_FILTER);
@@ -1053,20 +1037,7 @@ static int field_ptr(cs3d_handle *h, int field, double **p) {
             h->launches++;
         }
     }
-    else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) {
-        *p = h->q2.f[field - CS3D_F_RHO2];
-        if (h->acc_live) {
-            // mid-step in the mixed RK4 form: the accumulator is q1 + acc
-            ShadowArgs a{};
-            a.g = h->g;
-            a.q.f[0] = *p;
-            a.in[0] = h->racc[field - CS3D_F_RHO2];
-            a.base[0] = h->q1.f[field - CS3D_F_RHO2];
-            a.nf = 1;
-            CS3D_CUDA(launch_shadow(a, h->stream));
-            h->launches++;
-        }
-    }
+    else if (field >= CS3D_F_RHO2 && field < CS3D_F_RHO2 + 5) *p = h->q2.f[field - CS3D_F_RHO2];
     else if (field >= CS3D_F_RHOK2 && field < CS3D_F_RHOK2 + 5) {
         if (!h->store_dq) return fail(CS3D_ERR_STATE, "increments are kept only with CS3D_OPT_STORE_INCREMENTS");
         *p = h->dq[field - CS3D_F_RHOK2];
@@ -1890,7 +1861,6 @@ extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double
         CS3D_CUDA(cudaMemcpyAsync(grad_host + (size_t)f * n, QB[f], n * 8, cudaMemcpyDeviceToHost, h->stream));
     // back to the recorded final state
     if ((rc = adj_set_state(h, FIN))) return rc;
-    h->acc_live = 0;
     h->timeStep = h->adj_end_ts;
     h->filterTimeStep = h->adj_end_fts;
     CS3D_CUDA(cudaMemcpyAsync(h->scal, h->adj_end_scal, 2 * 8, cudaMemcpyHostToDevice, h->stream));

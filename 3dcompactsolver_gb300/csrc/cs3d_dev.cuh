@@ -46,50 +46,20 @@ struct LineOp {
 };
 
 // Loads of operator coefficients (a few kB per operator, read by every line
-// solve): read-only path with L1 evict-last priority, so that the tiles'
-// streaming loads do not push them out of L1.
-#ifndef CS3D_COEF_EVICT_LAST
-#define CS3D_COEF_EVICT_LAST 1
-#endif
-__device__ __forceinline__ float ldc(const float *p) {
-#if CS3D_COEF_EVICT_LAST
-    float v;
-    asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-#else
-    return __ldg(p);
-#endif
-}
-__device__ __forceinline__ double ldc(const double *p) {
-#if CS3D_COEF_EVICT_LAST
-    double v;
-    asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
-#else
-    return __ldg(p);
-#endif
-}
+// solve) through the read-only data path.
+__device__ __forceinline__ float ldc(const float *p) { return __ldg(p); }
+__device__ __forceinline__ double ldc(const double *p) { return __ldg(p); }
 
 // Four consecutive coefficients from a 16-byte aligned address in one or two
 // 128-bit loads.
 __device__ __forceinline__ void load4(const float *p, float v[4]) {
-#if CS3D_COEF_EVICT_LAST
-    asm("ld.global.nc.L1::evict_last.v4.f32 {%0, %1, %2, %3}, [%4];"
-        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "l"(p));
-#else
     const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
     v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-#endif
 }
 __device__ __forceinline__ void load4(const double *p, double v[4]) {
-#if CS3D_COEF_EVICT_LAST
-    asm("ld.global.nc.L1::evict_last.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "l"(p));
-    asm("ld.global.nc.L1::evict_last.v2.f64 {%0, %1}, [%2];" : "=d"(v[2]), "=d"(v[3]) : "l"(p + 2));
-#else
     const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
     const double2 b = __ldg(reinterpret_cast<const double2 *>(p + 2));
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-#endif
 }
 
 // Conserved variables of one state (five FP64 arrays, XYZ layout).

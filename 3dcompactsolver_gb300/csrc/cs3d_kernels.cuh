@@ -67,8 +67,8 @@ struct SweepArgs {
     int rk, rk_step;
     Q5 q1, q2, qk;
     const float *q1s[5];    // FP32 shadow of q1 (mixed RK4, stages 2-3)
-    float *acc[5];          // mixed RK4: FP32 sum of b_i dq_i over stages 1-3
-    int fluct_out;          // mixed RK4, last stage of a filtered step: acc <- q2 - fref (FP32)
+    float *fluct[5];        // mixed RK4: q2 - fref in FP32, the filter's first input
+    int fluct_out;          // mixed RK4, last stage of a filtered step: write fluct
     double fref[5];         // the filter's per-field reference values
     float *shadow_out[5];   // FP32 shadow of the next stage input (mixed)
     int shadow_target;      // ShadowTarget
@@ -165,8 +165,7 @@ struct ShadowArgs {
     Geom g;
     Q5 q;
     float *out[5];
-    const float *in[5];
-    const double *base[5];  // with in: q = base + in (FP64), else q = in
+    const float *in[5];     // set: q = widen(in); else out = narrow(q)
     int nf;
 };
 

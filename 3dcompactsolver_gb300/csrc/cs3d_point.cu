@@ -296,7 +296,7 @@ __global__ void k_shadow(ShadowArgs a) {
     for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
          gi += (long long)gridDim.x * blockDim.x) {
         for (int f = 0; f < a.nf; ++f) {
-            if (a.in[0]) a.q.f[f][gi] = a.base[0] ? a.base[f][gi] + widen(a.in[f][gi]) : widen(a.in[f][gi]);
+            if (a.in[0]) a.q.f[f][gi] = widen(a.in[f][gi]);
             else a.out[f][gi] = narrow(a.q.f[f][gi]);
         }
     }

@@ -44,14 +44,8 @@
 #ifndef CS3D_FMINB
 #define CS3D_FMINB 4   // resident blocks per SM the mixed filter is compiled for (64 registers)
 #endif
-#ifndef CS3D_ZC1
-#define CS3D_ZC1 2     // points per thread in flight in the z sweep's right-hand-side pass (batched form)
-#endif
 #ifndef CS3D_YC
 #define CS3D_YC 4      // points per thread in flight in the y sweep's consume phase
-#endif
-#ifndef CS3D_ZC1_PIPE
-#define CS3D_ZC1_PIPE 1  // the z sweep's right-hand-side pass software-pipelined (0: batched)
 #endif
 #ifndef CS3D_ZC2
 #define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
@@ -312,14 +306,13 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
     //   qa = q1 (RK4 stage 1, all TVD-RK3 stages) or q2 (RK4 stages 2-4)
     //   qb = q1 for the FP64 RK4 qk update on stages 2-3, or the FP64 qk of
     //        TVD-RK3 stages 2-3
-    //   mixed RK4: no FP64 state on stages 1-3 -- the increments b_i dq_i are
-    //   summed in FP32 (acc) and added to q1 once, on stage 4
-    const bool use_q1a = tvd || st == 1 || (a.mixed_rk4 && st == 4);
-    const bool need_qa = !(a.mixed_rk4 && st < 4);
+    //   mixed RK4: q2 accumulates every stage's increment in FP64; the next
+    //   stage input qk = q1 + b dq exists only as an FP32 shadow, formed from
+    //   q1's shadow (the stage input itself on stage 1)
+    const bool use_q1a = tvd || st == 1;
     const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
     const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
     const bool need_qs = a.mixed_rk4 && st == 1;
-    const bool need_acc = a.mixed_rk4 && st > 1;
     // Phase C runs in two passes over the same points, each point by the same
     // thread in both (so no barrier between them): C1 forms the right-hand
     // side and parks dq = dt*RHS in the point's own, now unused, solve slots;
@@ -331,11 +324,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
         T v[18];
         T qsv[5];
     };
-#if CS3D_ZC1_PIPE
     pipelined<InC1>(NL,
-#else
-    batched<InC1, CS3D_ZC1>(NL,
-#endif
         [&](InC1 &in, int p) {
             in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
@@ -417,7 +406,6 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
         Pt pt;
         double qa[5], qb[5];
         T qsv[5];    // q1's shadow: the stage input qs on stage 1, q1s on 2-3
-        float acc[5];
     };
     batched<InC2, CS3D_ZC2>(NL,
         [&](InC2 &in, int p) {
@@ -425,10 +413,9 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
             const unsigned gi = in.pt.gi;
 #pragma unroll
             for (int f = 0; f < 5; ++f) {
-                in.qa[f] = need_qa ? (use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi]) : 0.0;
+                in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
                 in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
                 in.qsv[f] = need_qs ? a.qs[f][gi] : need_q1s ? (T)a.q1s[f][gi] : T(0);
-                in.acc[f] = need_acc ? a.acc[f][gi] : 0.f;
             }
         },
         [&](InC2 &in) {
@@ -464,19 +451,18 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
                         else { nv = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
                         if (a.shadow_target != SHADOW_NONE) a.shadow_out[f][gi] = narrow(nv);
                     } else {
+                        // RK4: q2 += a_s dq in FP64 on every stage (RK4.hpp:35-118)
                         const T ca = (st == 1 || st == 4) ? T(1.0 / 6.0) : T(1.0 / 3.0);
                         const T cb = (st == 3) ? T(1.0) : T(0.5);
+                        const double q2n = in.qa[f] + to_f64(ca * d);
+                        a.q2.f[f][gi] = q2n;
                         if (st < 4) {
-                            // acc = sum of b_i dq_i so far; the next stage input
-                            // qk = q1 + cb*dq, kept as an FP32 shadow
-                            a.acc[f][gi] = st == 1 ? ca * d : fma(ca, d, (T)in.acc[f]);
+                            // the next stage input qk = q1 + cb*dq, kept as an FP32 shadow
                             a.shadow_out[f][gi] = fma(cb, d, in.qsv[f]);
                         } else {
-                            const double q2n = in.qa[f] + to_f64(fma(ca, d, (T)in.acc[f]));
-                            a.q2.f[f][gi] = q2n;
                             if (a.shadow_target == SHADOW_Q2) a.shadow_out[f][gi] = narrow(q2n);
                             // the filter's first pass input, q2 - fref in FP32
-                            if (a.fluct_out) a.acc[f][gi] = narrow(q2n - a.fref[f]);
+                            if (a.fluct_out) a.fluct[f][gi] = narrow(q2n - a.fref[f]);
                         }
                     }
                 }

@@ -25,7 +25,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -52,9 +51,11 @@ def kernel_bytes_per_point(kernel, wb, rk_stages):
     if kernel == "sweep_z":    # q*, prims, Ux..Tx, Uy..Ty, mu mu', R in, then the RK update
         common = wb * (5 + 5 + 4 + 4 + 2 + 5)
         if rk_stages == 4 and mixed:
-            # st1: qk, acc out; st2-3: acc, q1 shadow in, qk, acc out;
-            # st4: q1, acc in, q2 out, and q2 - fref for the filter (filtered steps)
-            per = [common + 40, common + 40 + 40, common + 40 + 40, common + 60 + 40 + 20]
+            # FP64 accumulation q2 += a_s dq on every stage, the next stage
+            # input as an FP32 shadow:  st1: q1 in, q2 + qk shadow out;
+            # st2-3: q2 + q1 shadow in, q2 + qk shadow out; st4: q2 in, q2 out
+            # plus either q2's shadow or q2 - fref (the filter's first input)
+            per = [common + 40 + 60, common + 60 + 60, common + 60 + 60, common + 40 + 60]
         elif rk_stages == 4:
             # st1: q1 in, q2 qk out; st2-3: q1 q2 in, q2 qk out; st4: q2 in, q2 out
             per = [common + 40 + 80, common + 80 + 80, common + 80 + 80, common + 40 + 40]
@@ -72,6 +73,45 @@ def kernel_bytes_per_point(kernel, wb, rk_stages):
         return (40 + 40 + (20 + 20 + 40 + 40 + 20)) / 3.0
     if kernel == "cfl":
         return 20.0 if mixed else 40.0
+    return 0.0
+
+
+# Algorithmic FP64 operations per grid point of one launch of the plain FP64
+# form on a periodic grid, counted from the kernel sources (cs3d_sweeps.cu,
+# cs3d_point.cu): an add, multiply, divide, square root or pow is one
+# operation, a fused multiply-add two.  One interior line solve with half
+# width H: the (2H+1)-tap right-hand side (2H+1 FMAs), the forward recurrence
+# (one FMA), the back substitution (one FMA and one multiply) and the
+# Sherman-Morrison correction on read (one FMA): 17 operations for the
+# derivatives (H = 2), 25 for the filter (H = 4).
+SOLVE_FLOPS_D = 17
+SOLVE_FLOPS_F = 25
+
+
+def kernel_flops_per_point(kernel, rk_stages):
+    """FP64 operations per grid point of one launch (plain form, periodic,
+    no sponge).  Breakdown:
+      sweep_x: primitives 10 + 4 div, fluxes 7, 13 solves, mu = mu_ref T^0.76
+               (pow + 1), mu' (1 + div), the five x-parts of the right-hand
+               side 17;
+      sweep_y: fluxes 7, 15 solves, the y-parts 31;
+      sweep_z: Uxz+Vyz and fluxes 8, 16 solves, the right-hand side with the
+               nonlinear viscous terms 158, dq = dt R 5, and the RK update
+               (RK4: 4 per field on stages 1-3, 2 on stage 4; TVD-RK3: 2, 5, 5);
+      filter:  5 solves of half width 4 per pass;
+      cfl:     primitives, sound speed and the three characteristic rates 16
+               + 7 div + sqrt."""
+    if kernel == "sweep_x":
+        return 17 + 4 + 13 * SOLVE_FLOPS_D + 2 + 2 + 17
+    if kernel == "sweep_y":
+        return 7 + 15 * SOLVE_FLOPS_D + 31
+    if kernel == "sweep_z":
+        rk = [20, 20, 20, 10] if rk_stages == 4 else [10, 25, 25]
+        return 8 + 16 * SOLVE_FLOPS_D + 158 + 5 + sum(rk) / len(rk)
+    if kernel == "filter":
+        return 5 * SOLVE_FLOPS_F
+    if kernel == "cfl":
+        return 16 + 7 + 1
     return 0.0
 
 
@@ -246,6 +286,13 @@ def cpu_baseline(workload, seconds=12.0):
                       f"(oracle/cs3d_oracle.c, -O3 -ffast-math -funroll-loops -fopenmp)"}
 
 
+def bench_config(desc, cfg, ws):
+    """The `config` object of both arms' JSON lines (the same workload)."""
+    return {"workload": desc, "npts": int(cfg.npts), "rk_stages": 3 if cfg.rk == 1 else 4,
+            "l2": "inputs larger than L2: the stage streams ~0.5-0.9 GB through HBM",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -282,11 +329,111 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "warmup": nw, "ms_per_step": round(1e3 * el / max(n, 1), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": desc, "npts": cfg.npts},
+            "data": "synthetic", "config": bench_config(desc, cfg, ws),
             "cpu_baseline": cb,
             "e2e": {"value": round(val, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def kernel_timing(solver, pkg, steps):
+    """{kernel class: (total ms, launches)} over `steps` steps, from CUDA
+    events around every launch on the library's stream."""
+    solver.set_option(pkg.OPT_KERNEL_TIMING, 1)
+    solver.kernel_times(reset=True)
+    solver.run(steps)
+    kt = solver.kernel_times(reset=True)
+    solver.set_option(pkg.OPT_KERNEL_TIMING, 0)
+    solver.sync()
+    return kt
+
+
+def roofline_of(kt, npts, steps, wb, stages, hbm_peak, peak_src, traffic_key=None):
+    """HBM roofline of the dominant kernel (algorithmic bytes per launch over
+    its average CUDA-event launch time), and the whole stage's fraction."""
+    dom = max((k for k in kt if kt[k][1] > 0), key=lambda k: kt[k][0])
+    avg_ms = kt[dom][0] / kt[dom][1]
+    bpp = kernel_bytes_per_point(dom, wb, stages)
+    achieved = bpp * npts / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "dram_bytes_per_point.json")
+    if traffic_key and os.path.exists(tr_path):
+        tr = json.load(open(tr_path))
+        if f"{traffic_key}:{dom}" in tr:
+            traffic = round(tr[f"{traffic_key}:{dom}"] * npts)
+    r = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
+         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+         "peak_source": peak_src, "bytes_per_point": bpp, "avg_launch_ms": round(avg_ms, 4),
+         "kernel_ms_per_step": {k: round(v[0] / steps, 4) for k, v in kt.items() if v[1]}}
+    return r
+
+
+def fp64_rate_tflops(torch):
+    """Measured FP64 arithmetic rate of this GPU: torch.matmul in float64
+    (cuBLAS DGEMM) of 4096^3, best of 3 after a warm-up, CUDA events."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
+
+
+def fp64_roofline(kt, npts, steps, stages, hbm_peak, peak_src, dgemm_tflops):
+    """Roofline of the plain FP64 form's dominant kernel against min(HBM roof,
+    FP64 roof): algorithmic bytes and algorithmic flops per launch (counted
+    from the kernel sources, kernel_flops_per_point) over the launch time."""
+    r = roofline_of(kt, npts, steps, 8, stages, hbm_peak, peak_src, "fp64")
+    dom = r["kernel"]
+    fpp = kernel_flops_per_point(dom, stages)
+    tflops = fpp * npts / (r["avg_launch_ms"] / 1e3) / 1e12
+    r["flops_per_point"] = fpp
+    r["fp64_achieved_tflops"] = round(tflops, 4)
+    r["fp64_peak_tflops"] = round(dgemm_tflops, 4)
+    r["fp64_peak_source"] = "measured: cuBLAS DGEMM 4096^3 through torch.matmul, burst"
+    r["fp64_frac"] = round(tflops / dgemm_tflops, 4)
+    # the binding roof: the time the kernel needs at the HBM roof or at the
+    # FP64 roof, whichever is longer, over its measured time
+    t_hbm = r["bytes_per_point"] * npts / (hbm_peak * 1e9)
+    t_fp = fpp * npts / (dgemm_tflops * 1e12)
+    r["bound"] = "fp64" if t_fp > t_hbm else "hbm"
+    r["roof_frac"] = round(max(t_hbm, t_fp) / (r["avg_launch_ms"] / 1e3), 4)
+    return r
+
+
+def hit256_leg(pkg, torch, steps, warmup):
+    """HIT 256^3 in both forms, device-resident, `warmup` + `steps` steps each
+    (the same step count, so the kinetic energies compare)."""
+    c = _cases()
+    abi = importlib.import_module("3dcompactsolver_gb300._abi")
+    cfg, ic = c.hit(256, precision=abi.FP32_MIXED)
+    out = {}
+    ke = {}
+    for prec in (abi.FP32_MIXED, abi.FP64):
+        cfg.precision = prec
+        s = pkg.Solver(cfg)
+        s.set_initial_conditions(*ic)
+        s.run(warmup)
+        s.sync()
+        ms = time_steps(s, steps, torch)
+        out[prec] = cfg.npts * 4 * steps / (ms / 1e3) / 1e6
+        ke[prec] = kinetic_energy(s.conserved())
+        s.close()
+    return {"workload": "decaying isotropic turbulence 256^3, RK4, Mt 0.3, E(k)~(k/8)^4 exp(-2(k/8)^2), seed 0",
+            "value": round(out[abi.FP32_MIXED], 3), "fp64_value": round(out[abi.FP64], 3), "unit": UNIT,
+            "mixed_over_fp64": round(out[abi.FP32_MIXED] / out[abi.FP64], 3),
+            "ke_rel_err_vs_fp64": float(abs(ke[abi.FP32_MIXED] - ke[abi.FP64]) / abs(ke[abi.FP64])),
+            "steps": steps, "warmup": warmup}
 
 
 def run_ours(args):
@@ -325,33 +472,14 @@ def run_ours(args):
     value = ws * npts * stages * args.steps / (ms / 1e3) / 1e6
 
     # per-kernel device times (events on the library's stream) for the roofline
-    s.set_option(pkg.OPT_KERNEL_TIMING, 1)
-    s.kernel_times(reset=True)
-    s.run(args.steps)
-    kt = s.kernel_times(reset=True)
-    s.set_option(pkg.OPT_KERNEL_TIMING, 0)
-    s.sync()
+    kt = kernel_timing(s, pkg, args.steps)
     peaks = {}
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    dom = max((k for k in kt if kt[k][1] > 0), key=lambda k: kt[k][0])
-    avg_ms = kt[dom][0] / kt[dom][1]
-    bpp = kernel_bytes_per_point(dom, wb, stages)
-    achieved = bpp * npts / (avg_ms / 1e3) / 1e9
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "dram_bytes_per_point.json")
-    if os.path.exists(tr_path):
-        tr = json.load(open(tr_path))
-        key = f"{args.precision}:{dom}"
-        if key in tr:
-            traffic = round(tr[key] * npts)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
-                "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
-                "peak_source": peak_src, "bytes_per_point": bpp, "avg_launch_ms": round(avg_ms, 4),
-                "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+    roofline = roofline_of(kt, npts, args.steps, wb, stages, hbm_peak, peak_src, args.precision)
     # stage-level fraction against the byte model of the whole stage
     stage_bytes = sum(kernel_bytes_per_point(k, wb, stages) * (kt[k][1] / args.steps)
                       for k in ("sweep_x", "sweep_y", "sweep_z", "filter", "cfl")) * npts
@@ -391,14 +519,26 @@ def run_ours(args):
         s3.sync()
         ke_m = kinetic_energy(s3.conserved() if args.precision == "mixed" else s2.conserved())
         ke_d = kinetic_energy(s2.conserved() if args.precision == "mixed" else s3.conserved())
+        s3.close()
         v2 = ws * npts * stages * args.steps / (ms2 / 1e3) / 1e6
-        other = {"other_form": {"precision": other_prec, "value": round(v2, 3), "unit": UNIT,
-                                "ms_per_step": round(ms2 / args.steps, 4)},
+        of = {"precision": other_prec, "value": round(v2, 3), "unit": UNIT,
+              "ms_per_step": round(ms2 / args.steps, 4)}
+        kt2 = kernel_timing(s2, pkg, args.steps)
+        s2.close()
+        if other_prec == "fp64":
+            of["roofline"] = fp64_roofline(kt2, npts, args.steps, stages, hbm_peak, peak_src,
+                                           fp64_rate_tflops(torch))
+        else:
+            of["roofline"] = roofline_of(kt2, npts, args.steps, 4, stages, hbm_peak, peak_src, "mixed")
+        other = {"other_form": of,
                  "mixed_over_fp64": round((value / v2) if args.precision == "mixed" else (v2 / value), 3),
                  "ke_rel_err_vs_fp64": float(abs(ke_m - ke_d) / abs(ke_d)),
                  "ke_steps": args.warmup + args.steps}
-        s2.close()
-        s3.close()
+
+    # HIT 256^3 in both forms (the second grid the mixed/FP64 ratio is quoted on)
+    hit = None
+    if not args.no_hit and args.workload != "hit256":
+        hit = hit256_leg(pkg, torch, args.hit_steps, args.warmup)
 
     # the discrete adjoint of the same workload (periodic RK4 only): record
     # `steps` steps at the current dt frozen, then the backward sweep
@@ -423,25 +563,25 @@ def run_ours(args):
                    "backward_ms_per_step": round(back_s * 1e3 / args.steps, 3),
                    "backward_over_forward": round(back_s * 1e3 / ms, 2),
                    "value": round(ws * npts * args.steps / back_s / 1e6, 3),
-                   "unit": "Mpts x steps / s (backward sweep)",
-                   "check": "profiles/adjoint_tgv128.md (16 directions vs central differences)"}
+                   "unit": "Mpts x steps / s (backward sweep)"}
 
     cb = cpu_baseline(args.workload) if (rank == 0 and ws == 1 and not args.no_cpu) else None
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
-            "precision": ("FP32-mixed: FP32 derivative/RHS/flux/filter arithmetic; FP64 state, RK "
-                          "accumulation and Sherman-Morrison factor") if args.precision == "mixed"
+            "precision": ("FP32-mixed: FP32 derivative/RHS/flux/filter arithmetic; FP64 conserved state, "
+                          "RK accumulation q2 += a_s dq on every stage and Sherman-Morrison factor; "
+                          "the RK4 stage input qk as an FP32 shadow") if args.precision == "mixed"
                          else "FP64 throughout",
             "data": "synthetic",
-            "config": {"workload": desc, "npts": npts, "rk_stages": stages,
-                       "l2": "inputs larger than L2: the stage streams ~0.5-0.9 GB through HBM",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU"},
+            "config": bench_config(desc, cfg, ws),
             "clocks": clocks, "roofline": roofline, "cpu_baseline": cb,
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": 5 * 8 * npts,
                     "d2h_bytes_per_step": 5 * 8 * npts},
             "gpu_launches": int(launches)}
     line.update(other)
+    if hit is not None:
+        line["hit256"] = hit
     if adjoint is not None:
         line["adjoint"] = adjoint
     s.close()
@@ -464,6 +604,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the other form and the KE error")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint timing")
+    ap.add_argument("--no-hit", action="store_true", help="skip the HIT 256^3 leg")
+    ap.add_argument("--hit-steps", type=int, default=10, help="timed steps of the HIT 256^3 leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -1,6 +1,6 @@
 """Check the discrete adjoint on the Taylor-Green vortex.
 
-    python 3dcompactsolver_gb300/check_adjoint.py --N 128 --steps 200 --dirs 16
+    python check_adjoint.py --N 128 --steps 200 --dirs 16
 
 J = volume-averaged kinetic energy after `steps` RK4 steps at a fixed time
 step (the CFL 0.5 step of the initial state).  The gradient dJ/d(U0, V0, W0)
@@ -19,7 +19,7 @@ import time
 
 import numpy as np
 
-sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 cs3d = importlib.import_module("3dcompactsolver_gb300")
 cases = importlib.import_module("3dcompactsolver_gb300.cases")
 

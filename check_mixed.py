@@ -1,7 +1,7 @@
 """Kinetic-energy and dissipation error of the FP32-mixed form against the
 FP64 form, per workload.
 
-    python 3dcompactsolver_gb300/check_mixed.py [--workloads tgv128,hit256,shear]
+    python check_mixed.py [--workloads tgv128,hit256,shear]
 
 Both forms run the same initial state with CFL time steps.  Every `every`
 steps the diagnostics of calcTaylorGreenQuantities (CSolver_AWS.cpp:
@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 
-sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 cs3d = importlib.import_module("3dcompactsolver_gb300")
 cases = importlib.import_module("3dcompactsolver_gb300.cases")
 

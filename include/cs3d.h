@@ -52,8 +52,11 @@ extern "C" {
 /* arithmetic of the stage */
 #define CS3D_FP64        0  /* plain form: every operation in FP64        */
 #define CS3D_FP32_MIXED  1  /* RHS, flux, derivative and filter arithmetic in
-                               FP32; conserved state, RK accumulation and the
-                               cyclic Sherman-Morrison factor in FP64       */
+                               FP32; conserved state q1/q2, the RK
+                               accumulation q2 += a_s dq of every stage and
+                               the cyclic Sherman-Morrison factor in FP64;
+                               the RK4 stage input qk = q1 + b_s dq is kept
+                               as an FP32 shadow only                       */
 /* sponge construction */
 #define CS3D_SPONGE_REFERENCE 0 /* sigma built only on SPONGE faces with the
                                    reference's band widths 0.25Lx, 0.125Ly,
@@ -91,11 +94,7 @@ typedef struct cs3d_config {
 #define CS3D_F_RHOW1  3
 #define CS3D_F_RHOE1  4
 #define CS3D_F_RHOK   5   /* rhok..rhoEk: stage input (qk)      5..9  */
-#define CS3D_F_RHO2   10  /* rho2..rhoE2: RK accumulator (q2)  10..14;
-                             between the stages of an FP32-mixed RK4 step the
-                             accumulator is q1 plus an FP32 sum of the stage
-                             increments: reads form that sum, writes there do
-                             not reach the step's last stage */
+#define CS3D_F_RHO2   10  /* rho2..rhoE2: RK accumulator (q2)  10..14 */
 #define CS3D_F_RHOK2  15  /* rhok2..rhoEk2: last increment dq  15..19 */
 #define CS3D_F_U      20  /* U V W p T mu sos from q1 (the solver's
                              primitives after the last stage)  20..26 */

@@ -32,17 +32,24 @@ def _ptr(a):
     return a.ctypes.data_as(_DP)
 
 
+def reference_dir():
+    """The reference checkout that oracle/Makefile compiles from (its REF,
+    which $CS3D_REFERENCE overrides), or None where that directory does not
+    exist (the GPU machines carry no reference checkout)."""
+    import subprocess
+    out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    d = out.stdout.strip()
+    return d if out.returncode == 0 and d and os.path.isdir(d) else None
+
+
 def build(ref=False, quiet=True):
     """Compile the restatement (and, with ref=True and a reference checkout
     present, the reference harness)."""
     import subprocess
     targets = ["all"]
-    if ref and os.path.isdir(os.environ.get("CS3D_REFERENCE", "/root/reference")):
+    if ref and reference_dir():
         targets.append("ref")
-    env = dict(os.environ)
-    if "CS3D_REFERENCE" in os.environ:
-        env["REF"] = os.environ["CS3D_REFERENCE"]
-    out = subprocess.run(["make", "-C", HERE] + targets, capture_output=True, text=True, env=env)
+    out = subprocess.run(["make", "-C", HERE] + targets, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

@@ -20,8 +20,10 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
+    """The oracle, built; where the reference checkout exists (never on the
+    GPU machines) its own sources are built beside it for the pinning tests."""
     import oracle as o
-    o.build()
+    o.build(ref=True)
     return o
 
 

@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures of tests/golden from the reference.
 
-Needs the reference checkout (default /root/reference, or $CS3D_REFERENCE)
+Needs the reference checkout (oracle/Makefile's REF, or $CS3D_REFERENCE)
 and the reference harness built by `make -C oracle ref`.  Writes:
 
   taylorgreen_run64_head.txt   rows 1-5 of taylorgreen_vortex/taylorgreen_run64/taylorgreen.out
@@ -27,7 +27,9 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle  # noqa: E402
 
-REF = os.environ.get("CS3D_REFERENCE", "/root/reference")
+REF = oracle.reference_dir()
+if REF is None:
+    raise SystemExit("make_golden.py: no reference checkout (set REF in oracle/Makefile or $CS3D_REFERENCE)")
 cases = importlib.import_module("3dcompactsolver_gb300.cases")
 _abi = importlib.import_module("3dcompactsolver_gb300._abi")
 

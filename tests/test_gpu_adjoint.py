@@ -153,9 +153,21 @@ def test_adjoint_rejects_unsupported(gpu_pkg, cases):
     assert e.value.code == 6
 
 
+def _smooth(rng, N, kmax=4.0):
+    """A seeded random field with its energy at wavenumbers up to about kmax."""
+    k = np.fft.fftfreq(N, d=1.0 / N)
+    KZ, KY, KX = np.meshgrid(k, k, k, indexing="ij")
+    f = np.real(np.fft.ifftn(np.fft.fftn(rng.standard_normal((N, N, N))) *
+                             np.exp(-(KX ** 2 + KY ** 2 + KZ ** 2) / (kmax * kmax))))
+    return f / np.sqrt(np.mean(f * f))
+
+
 def test_mixed_adjoint_tracks_fp64(gpu_pkg, cases):
     """The FP32-mixed adjoint (FP32 stage Jacobians at the mixed forward's
-    stage inputs) against the FP64 adjoint and FP64 finite differences."""
+    stage inputs, FP64 adjoint state and RK combination) against the FP64
+    adjoint, and against central differences of the FP64 forward on three
+    smooth seeded directions: within 1e-6 relative, the bound the adjoint is
+    held to (TGV 24^3, 8 RK4 steps, filter every step)."""
     N, nsteps = 24, 8
     cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
     cfg_m, _ = cases.tgv(N, precision=gpu_pkg.FP32_MIXED)
@@ -170,15 +182,18 @@ def test_mixed_adjoint_tracks_fp64(gpu_pkg, cases):
         s.close()
     num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(grads[1], grads[0])))
     den = np.sqrt(sum(np.sum(b * b) for b in grads[0]))
-    assert num / den <= 1e-4, num / den
+    assert num / den <= 1e-5, num / den
     rng = np.random.default_rng(11)
     rho0, p0, U0, V0, W0 = ic
     eps = 1e-5
-    dU, dV, dW = (rng.standard_normal(U0.shape) for _ in range(3))
-    fd = (_forward_J(gpu_pkg, cfg, (rho0, p0, U0 + eps * dU, V0 + eps * dV, W0 + eps * dW), nsteps)
-          - _forward_J(gpu_pkg, cfg, (rho0, p0, U0 - eps * dU, V0 - eps * dV, W0 - eps * dW), nsteps)) / (2 * eps)
-    am = float(np.sum(grads[1][0] * dU + grads[1][1] * dV + grads[1][2] * dW))
-    assert abs(am - fd) <= 1e-4 * abs(fd), (am, fd)
+    for _ in range(3):
+        dU, dV, dW = (_smooth(rng, N) for _ in range(3))
+        fd = (_forward_J(gpu_pkg, cfg, (rho0, p0, U0 + eps * dU, V0 + eps * dV, W0 + eps * dW), nsteps)
+              - _forward_J(gpu_pkg, cfg, (rho0, p0, U0 - eps * dU, V0 - eps * dV, W0 - eps * dW), nsteps)) / (2 * eps)
+        a64 = float(np.sum(grads[0][0] * dU + grads[0][1] * dV + grads[0][2] * dW))
+        am = float(np.sum(grads[1][0] * dU + grads[1][1] * dV + grads[1][2] * dW))
+        assert abs(a64 - fd) <= 1e-8 * abs(fd), (a64, fd)
+        assert abs(am - fd) <= 1e-6 * abs(fd), (am, fd, abs(am - fd) / abs(fd))
 
 
 def test_mixed_rhs_vjp_tracks_fp64(gpu_pkg, cases):

@@ -83,11 +83,10 @@ def test_port_reproduces_taylorgreen_run64(oracle, cases):
         assert abs(q[6] - gold[6]) <= 1e-10 * abs(gold[6])  # rms dilatation: a tiny quantity
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
-                                                    "libref3d_strict.so")),
-                    reason="reference harness not built here (no reference checkout)")
 @pytest.mark.parametrize("name", ["wall_moving_sponge", "shear"])
 def test_port_bit_identical_to_live_reference(oracle, cases, name):
+    if not oracle.ref_available():
+        pytest.skip("reference harness not built here (no reference checkout)")
     cfg, ic = _case(cases, name)
     p = oracle.OraclePort(cfg)
     r = oracle.RefSolver(cfg)
