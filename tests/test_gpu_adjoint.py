@@ -164,10 +164,16 @@ def _smooth(rng, N, kmax=4.0):
 
 def test_mixed_adjoint_tracks_fp64(gpu_pkg, cases):
     """The FP32-mixed adjoint (FP32 stage Jacobians at the mixed forward's
-    stage inputs, FP64 adjoint state and RK combination) against the FP64
-    adjoint, and against central differences of the FP64 forward on three
-    smooth seeded directions: within 1e-6 relative, the bound the adjoint is
-    held to (TGV 24^3, 8 RK4 steps, filter every step)."""
+    stage inputs, FP64 adjoint state and RK combination) within 1e-6, the
+    bound the adjoint is held to (TGV 24^3, 8 RK4 steps, filter every step):
+
+    * its velocity gradient against the FP64 adjoint's, relative L2 norm;
+    * its directional derivatives against central differences of the FP64
+      forward on seeded smooth directions.  A directional derivative g.d is
+      only as well determined as |g||d| / |g.d| allows (a direction nearly
+      orthogonal to the gradient amplifies every rounding error, the FP64
+      adjoint's too), so directions with |g.d| < |g||d| / 100 are drawn again;
+      at least three directions are checked."""
     N, nsteps = 24, 8
     cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N)
     cfg_m, _ = cases.tgv(N, precision=gpu_pkg.FP32_MIXED)
@@ -181,19 +187,27 @@ def test_mixed_adjoint_tracks_fp64(gpu_pkg, cases):
         grads.append(gpu_pkg.ic_velocity_gradient(g, ic[0], ic[2], ic[3], ic[4]))
         s.close()
     num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(grads[1], grads[0])))
-    den = np.sqrt(sum(np.sum(b * b) for b in grads[0]))
-    assert num / den <= 1e-5, num / den
+    gnorm = np.sqrt(sum(np.sum(b * b) for b in grads[0]))
+    assert num / gnorm <= 1e-6, num / gnorm
     rng = np.random.default_rng(11)
     rho0, p0, U0, V0, W0 = ic
     eps = 1e-5
-    for _ in range(3):
+    checked = 0
+    for _ in range(12):
         dU, dV, dW = (_smooth(rng, N) for _ in range(3))
+        a64 = float(np.sum(grads[0][0] * dU + grads[0][1] * dV + grads[0][2] * dW))
+        dnorm = np.sqrt(np.sum(dU * dU) + np.sum(dV * dV) + np.sum(dW * dW))
+        if abs(a64) < gnorm * dnorm / 100:
+            continue
         fd = (_forward_J(gpu_pkg, cfg, (rho0, p0, U0 + eps * dU, V0 + eps * dV, W0 + eps * dW), nsteps)
               - _forward_J(gpu_pkg, cfg, (rho0, p0, U0 - eps * dU, V0 - eps * dV, W0 - eps * dW), nsteps)) / (2 * eps)
-        a64 = float(np.sum(grads[0][0] * dU + grads[0][1] * dV + grads[0][2] * dW))
         am = float(np.sum(grads[1][0] * dU + grads[1][1] * dV + grads[1][2] * dW))
         assert abs(a64 - fd) <= 1e-8 * abs(fd), (a64, fd)
         assert abs(am - fd) <= 1e-6 * abs(fd), (am, fd, abs(am - fd) / abs(fd))
+        checked += 1
+        if checked == 3:
+            break
+    assert checked == 3
 
 
 def test_mixed_rhs_vjp_tracks_fp64(gpu_pkg, cases):
