@@ -31,6 +31,7 @@ LIB_PATH = os.environ.get("CS3D_LIB_PATH") or os.path.join(HERE, "libcs3d_gb300.
 OPT_STORE_INCREMENTS = 1
 OPT_STORE_DIAGNOSTICS = 2
 OPT_KERNEL_TIMING = 3
+OP_DERIV1, OP_DERIV2, OP_FILTER = 1, 2, 3  # kinds of the operator-only handle
 ADJ_SEED = 0       # cs3d_adjoint_backward: dJ/dq of the final state given
 ADJ_KE_MEAN = 1    # J = mean over points of rho |u|^2 / 2 of the final state
 KERNEL_CLASSES = ("sweep_x", "sweep_y", "sweep_z", "filter", "boundary", "cfl", "sponge", "other")
@@ -89,6 +90,11 @@ def lib():
         L.cs3d_adjoint_backward.argtypes = [_H, ctypes.c_int, _DP, _DP, _DP]
         L.cs3d_rhs_eval.argtypes = [_H, _DP, _DP]
         L.cs3d_rhs_vjp.argtypes = [_H, _DP, _DP, _DP]
+        L.cs3d_op_create.argtypes = [ctypes.POINTER(Config), ctypes.c_int, ctypes.POINTER(_H)]
+        L.cs3d_op_destroy.argtypes = [_H]
+        L.cs3d_op_apply.argtypes = [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.cs3d_op_apply_host.argtypes = [_H, ctypes.c_int, _DP, _DP]
+        L.cs3d_op_get_stream.argtypes = [_H, ctypes.POINTER(ctypes.c_void_p)]
         _lib = L
     return _lib
 
@@ -280,6 +286,49 @@ class Solver:
         check(fn(self.h, int(direction), ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr)))
 
 
+class Operator:
+    """An operator-only handle (cs3d_op_*): the 1st-derivative, 2nd-derivative
+    and filter operators of one direction of the grid in cfg, with no solver
+    state.  kind 1/2/3 = OP_DERIV1 / OP_DERIV2 / OP_FILTER."""
+
+    def __init__(self, cfg, direction):
+        h = _H()
+        check(lib().cs3d_op_create(ctypes.byref(cfg), int(direction), ctypes.byref(h)))
+        self.h = h
+        self.npts = cfg.Nx * cfg.Ny * cfg.Nz
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cs3d_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply(self, kind, in_ptr, out_ptr):
+        """Device arrays (integer addresses), queued on stream()."""
+        check(lib().cs3d_op_apply(self.h, int(kind), ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr)))
+
+    def apply_host(self, kind, data_in, data_out=None):
+        """Host arrays, synchronous; returns data_out (allocated if None)."""
+        a = np.ascontiguousarray(data_in, dtype=np.float64)
+        if a.size != self.npts:
+            raise ValueError(f"field has {a.size} points, expected {self.npts}")
+        out = np.empty_like(a) if data_out is None else data_out
+        if not (out.flags.c_contiguous and out.dtype == np.float64 and out.size == self.npts):
+            raise ValueError("data_out must be a C-contiguous float64 array of the field's size")
+        check(lib().cs3d_op_apply_host(self.h, int(kind), _dptr(a), _dptr(out)))
+        return out
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().cs3d_op_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+
 def ic_velocity_gradient(grad_q0, rho0, U0, V0, W0):
     """dJ/dU0, dJ/dV0, dJ/dW0 from dJ/dq0 through the initial state
     q0 = (rho0, rho0 U0, rho0 V0, rho0 W0, p0/(gamma-1) + rho0 |u0|^2 / 2)
@@ -446,10 +495,11 @@ class TVDRK3(_RKBase):
 
 
 class Derivatives:
-    """Derivatives(dom, bcType, dir): calc1stDerivField / calc2ndDerivField on
-    device arrays (integer device addresses) in the direction's contiguous
-    layout (Derivatives.cpp:3-96).  A private solver handle carries the
-    precomputed operators."""
+    """Derivatives(dom, bcType, dir) (Derivatives.hpp:54): calc1stDerivField /
+    calc2ndDerivField (Derivatives.cpp:3-96) on fields in the direction's
+    contiguous layout -- numpy arrays (synchronous, as the reference's host
+    arrays; dataOut is written in place) or integer device addresses (queued
+    on the operator handle's stream).  Backed by an operator-only handle."""
     DIRX, DIRY, DIRZ = DIRX, DIRY, DIRZ
 
     def __init__(self, dom, bcType, currentDir, alphaF=0.49):
@@ -457,21 +507,27 @@ class Derivatives:
         bt[currentDir] = bcType
         cfg = make_config((dom.Nx, dom.Ny, dom.Nz), (dom.Lx, dom.Ly, dom.Lz), bc_type=tuple(bt),
                           alphaF=alphaF)
-        self.solver = Solver(cfg)
+        self.op = Operator(cfg, currentDir)
         self.currentDir = currentDir
 
+    def _apply(self, kind, dataIn, dataOut):
+        if isinstance(dataIn, np.ndarray):
+            self.op.apply_host(kind, dataIn, dataOut)
+        else:
+            self.op.apply(kind, dataIn, dataOut)
+
     def calc1stDerivField(self, dataIn, dataOut):
-        self.solver.line_op(1, self.currentDir, dataIn, dataOut)
+        self._apply(OP_DERIV1, dataIn, dataOut)
 
     def calc2ndDerivField(self, dataIn, dataOut):
-        self.solver.line_op(2, self.currentDir, dataIn, dataOut)
+        self._apply(OP_DERIV2, dataIn, dataOut)
 
 
 class Filter(Derivatives):
-    """Filter(alphaF, dom, bcType, dir).filterField (Filter.cpp:129-171)."""
+    """Filter(alphaF, dom, bcType, dir).filterField (Filter.hpp:31, Filter.cpp:129-171)."""
 
     def __init__(self, alphaF, dom, bcType, currentDir):
         super().__init__(dom, bcType, currentDir, alphaF=alphaF)
 
     def filterField(self, dataIn, dataOut):
-        self.solver.line_op(3, self.currentDir, dataIn, dataOut)
+        self._apply(OP_FILTER, dataIn, dataOut)

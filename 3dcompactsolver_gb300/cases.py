@@ -174,3 +174,30 @@ def wall_box(N=(20, 18, 16), seed=1, precision=_abi.FP64, rk=_abi.RK4, moving=Fa
     W0 = 0.05 * np.sin(X * 2.0 + ph[4]) * np.cos(Z + ph[5])
     p = (1.0 / GAMMA) * (1.0 + 0.02 * np.cos(X + Y + Z))
     return cfg, (rho0, p, U0, V0, W0)
+
+
+def postprocess_grid():
+    """The grid of the reference's post-processor (PostProcess.cpp:44-79):
+    512 x 256 x 128 points over 345 x 172 x 86, x and z periodic, y solved
+    with the wall closures (its faces there are SPONGE kinds, which only the
+    solver uses; ADIABATIC_WALL here, so no sponge is built).  Returns
+    (config, conserved state q of shape (5, Nz, Ny, Nx)) with a smooth
+    analytic shear-layer-like state: a tanh profile in y with three-
+    dimensional perturbations, rho and p varying."""
+    cfg = _abi.make_config(
+        (512, 256, 128), (345.0, 172.0, 86.0),
+        bc_type=(_abi.PERIODIC_SOLVE, _abi.DIRICHLET_SOLVE, _abi.PERIODIC_SOLVE),
+        bc_kind=(_abi.PERIODIC, _abi.PERIODIC, _abi.ADIABATIC_WALL, _abi.ADIABATIC_WALL,
+                 _abi.PERIODIC, _abi.PERIODIC),
+        alphaF=0.49, mu_ref=0.0035, CFL=0.5)
+    X, Y, Z = _mesh(cfg)
+    ax, ay, az = 2.0 * math.pi * X / cfg.Lx, Y / cfg.Ly, 2.0 * math.pi * Z / cfg.Lz
+    env = np.exp(-((Y - cfg.Ly / 2.0) / 20.0) ** 2)
+    rho = 1.0 + 0.1 * np.sin(2.0 * ax + 0.3) * np.cos(math.pi * ay) * np.cos(az)
+    U = 0.5 * np.tanh((Y - cfg.Ly / 2.0) / 6.0) + 0.05 * env * np.sin(3.0 * ax) * np.sin(2.0 * az + 0.7)
+    V = 0.03 * env * np.cos(5.0 * ax + 0.2) * np.cos(az) + 0.01 * np.sin(math.pi * ay) * np.sin(ax)
+    W = 0.02 * (1.0 - (2.0 * ay - 1.0) ** 2) * np.sin(ax + 2.0 * az)
+    p = (1.0 / GAMMA) * (1.0 + 0.01 * np.cos(ax) * np.cos(3.0 * math.pi * ay))
+    rhoE = p / (GAMMA - 1.0) + 0.5 * rho * (U * U + V * V + W * W)
+    q = np.stack([rho, rho * U, rho * V, rho * W, rhoE])
+    return cfg, q

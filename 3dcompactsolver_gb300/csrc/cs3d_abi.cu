@@ -8,7 +8,6 @@
 #include <vector>
 #include <algorithm>
 #include <cstdlib>
-#include <mutex>
 #include <initializer_list>
 
 #include "../../include/cs3d.h"
@@ -1239,6 +1238,118 @@ extern "C" int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double
 }
 
 // ---------------------------------------------------------------------
+// operator-only handles: one direction's three compact operators
+// ---------------------------------------------------------------------
+struct cs3d_op {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    long long npts = 0;
+    DevOp<double> ops[3];
+    double *stage = nullptr;  // 2 * npts doubles for the host-array calls (allocated on first use)
+};
+
+extern "C" int cs3d_op_create(const cs3d_config *cfg, int dir, cs3d_op **out) {
+    if (!out) return fail(CS3D_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!cfg) return fail(CS3D_ERR_ARG, "null config");
+    if (dir < 0 || dir > 2) return fail(CS3D_ERR_ARG, "dir=%d", dir);
+    const int Nd[3] = {cfg->Nx, cfg->Ny, cfg->Nz};
+    const double Ld[3] = {cfg->Lx, cfg->Ly, cfg->Lz};
+    for (int d = 0; d < 3; d++)
+        if (Nd[d] < 1) return fail(CS3D_ERR_SHAPE, "N[%d]=%d", d, Nd[d]);
+    if (Nd[dir] < 8) return fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line needs at least 8 points", dir, Nd[dir]);
+    if (Nd[dir] > 4096) return fail(CS3D_ERR_SHAPE, "N[%d]=%d exceeds 4096 points per line", dir, Nd[dir]);
+    if ((long long)Nd[0] * Nd[1] * Nd[2] >= (1ll << 31))
+        return fail(CS3D_ERR_SHAPE, "Nx*Ny*Nz must stay below 2^31 points (32-bit indexing)");
+    if (!(Ld[dir] > 0.0)) return fail(CS3D_ERR_ARG, "L[%d] must be positive", dir);
+    const int bc = cfg->bc_type[dir];
+    if (bc != CS3D_PERIODIC_SOLVE && bc != CS3D_DIRICHLET_SOLVE)
+        return fail(CS3D_ERR_ARG, "bc_type[%d]=%d is not PERIODIC_SOLVE or DIRICHLET_SOLVE", dir, bc);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(CS3D_ERR_NODEV, "no CUDA device");
+    cs3d_op *o = new cs3d_op();
+    o->npts = (long long)Nd[0] * Nd[1] * Nd[2];
+    auto fail_free = [&](int code) {
+        cs3d_op_destroy(o);
+        return code;
+    };
+    if (cudaGetDevice(&o->dev) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail_free(fail(CS3D_ERR_CUDA, "stream creation failed"));
+    // Domain.hpp:31-45: dx = x[1] - x[0]
+    const double dh = (1.0 / ((double)Nd[dir] - 1.0)) * Ld[dir] - 0.0;
+    for (int k = 1; k <= 3; k++) {
+        int r = upload_op<double>(make_op(k, Nd[dir], bc, dh, cfg->alphaF), o->ops[k - 1], o->stream);
+        if (r) return fail_free(r);
+    }
+    if (cudaStreamSynchronize(o->stream) != cudaSuccess)
+        return fail_free(fail(CS3D_ERR_CUDA, "operator upload failed"));
+    *out = o;
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_op_destroy(cs3d_op *o) {
+    if (!o) return CS3D_OK;
+    DeviceGuard dg(o->dev);
+    if (o->stream) cudaStreamSynchronize(o->stream);
+    for (auto &d : o->ops)
+        if (d.mem) cudaFree(d.mem);
+    if (o->stage) cudaFree(o->stage);
+    if (o->stream) cudaStreamDestroy(o->stream);
+    delete o;
+    return CS3D_OK;
+}
+
+static int op_launch(cs3d_op *o, int kind, const double *in, double *out) {
+    LineOpArgs a{};
+    a.op = o->ops[kind - 1].op;
+    const int N = a.op.N;
+    a.nlines = o->npts / N;
+    a.L = 32;
+    while (a.L > 1 && sweep_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
+    a.P = a.L + 1;
+    a.threads = 128;
+    a.in = in;
+    a.out = out;
+    CS3D_CUDA(launch_line_op(a, o->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_op_apply(cs3d_op *o, int kind, const double *in_dev, double *out_dev) {
+    if (!o || !in_dev || !out_dev) return fail(CS3D_ERR_ARG, "null argument");
+    if (kind < CS3D_OP_DERIV1 || kind > CS3D_OP_FILTER) return fail(CS3D_ERR_ARG, "kind=%d", kind);
+    if (in_dev == out_dev) return fail(CS3D_ERR_ARG, "in and out must not overlap");
+    DeviceGuard dg(o->dev);
+    return op_launch(o, kind, in_dev, out_dev);
+}
+
+extern "C" int cs3d_op_apply_host(cs3d_op *o, int kind, const double *in_host, double *out_host) {
+    if (!o || !in_host || !out_host) return fail(CS3D_ERR_ARG, "null argument");
+    if (kind < CS3D_OP_DERIV1 || kind > CS3D_OP_FILTER) return fail(CS3D_ERR_ARG, "kind=%d", kind);
+    DeviceGuard dg(o->dev);
+    const size_t bytes = (size_t)o->npts * 8;
+    if (!o->stage) {
+        cudaError_t e = cudaMalloc(&o->stage, 2 * bytes);
+        if (e != cudaSuccess) {
+            o->stage = nullptr;
+            return fail(CS3D_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", 2 * bytes, cudaGetErrorString(e));
+        }
+    }
+    CS3D_CUDA(cudaMemcpyAsync(o->stage, in_host, bytes, cudaMemcpyHostToDevice, o->stream));
+    int rc = op_launch(o, kind, o->stage, o->stage + o->npts);
+    if (rc) return rc;
+    CS3D_CUDA(cudaMemcpyAsync(out_host, o->stage + o->npts, bytes, cudaMemcpyDeviceToHost, o->stream));
+    CS3D_CUDA(cudaStreamSynchronize(o->stream));
+    return CS3D_OK;
+}
+
+extern "C" int cs3d_op_get_stream(cs3d_op *o, void **stream) {
+    if (!o || !stream) return fail(CS3D_ERR_ARG, "null argument");
+    *stream = (void *)o->stream;
+    return CS3D_OK;
+}
+
+// ---------------------------------------------------------------------
 // Taylor-Green diagnostics
 // ---------------------------------------------------------------------
 template <typename T>
@@ -1421,12 +1532,6 @@ extern "C" int cs3d_aero_optics(cs3d_handle *h, int num_angles, double max_angle
 // ---------------------------------------------------------------------
 // allocation-free kinetic energy (no handle, no cudaMalloc, no host heap)
 // ---------------------------------------------------------------------
-namespace {
-constexpr int kKeMaxDevices = 64;
-std::mutex g_ke_mu;
-double *g_ke_ptr[kKeMaxDevices] = {};
-}  // namespace
-
 extern "C" int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *rhoU_dev,
                                            const double *rhoV_dev, const double *rhoW_dev,
                                            long long npts, void *stream, double *ke) {
@@ -1436,9 +1541,6 @@ extern "C" int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *
                     npts);
     int dev = -1;
     CS3D_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kKeMaxDevices)
-        return fail(CS3D_ERR_ARG, "device %d: the allocation-free kinetic energy serves devices 0..%d", dev,
-                    kKeMaxDevices - 1);
     const double *ptrs[4] = {rho_dev, rhoU_dev, rhoV_dev, rhoW_dev};
     for (int f = 0; f < 4; ++f) {
         cudaPointerAttributes at{};
@@ -1446,17 +1548,10 @@ extern "C" int cs3d_kinetic_energy_noalloc(const double *rho_dev, const double *
         if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != dev)
             return fail(CS3D_ERR_ARG, "array %d is not device memory of the current device %d", f, dev);
     }
+    // the static scratch array's address on the current device, looked up on
+    // every call: a device reset reloads the device code and can move it
     double *scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_ke_mu);
-        if (!g_ke_ptr[dev]) {
-            // first call on this device: look up the static scratch once
-            double *p = nullptr;
-            CS3D_CUDA(ke_scratch_address(&p));
-            g_ke_ptr[dev] = p;
-        }
-        scratch = g_ke_ptr[dev];
-    }
+    CS3D_CUDA(ke_scratch_address(&scratch));
     cudaStream_t s = (cudaStream_t)stream;
     CS3D_CUDA(launch_ke_noalloc(rho_dev, rhoU_dev, rhoV_dev, rhoW_dev, npts, scratch, s));
     CS3D_CUDA(cudaMemcpyAsync(ke, scratch + kKeBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -12,7 +12,12 @@
 //   RK4(cs), TVDRK3(cs): executeSolverLoop(), updateConservedData()
 //                                                            AbstractRK.hpp:13-14
 //   Derivatives_GB300(dom, bcType, dir).calc1stDerivField / calc2ndDerivField
-//   Filter_GB300(alphaF, dom, bcType, dir).filterField      (device arrays)
+//   Filter_GB300(alphaF, dom, bcType, dir).filterField      (host arrays, as
+//       the reference's; *_dev forms on device arrays)
+//
+// These classes stand alone (no reference headers needed).  For the
+// reference's own AbstractCSolver / RK4 / TVDRK3 classes see
+// cs3d_ref_binding.hpp.
 //
 // The five stage virtuals of the reference (preSubStep, solveEqnSet,
 // postSubStep, updateConservedData, updateData) run on the GPU as one fused
@@ -211,12 +216,17 @@ class TVDRK3 : public AbstractRK_GB300 {
     explicit TVDRK3(CSolver_GB300 *cs_) : AbstractRK_GB300(cs_, 3) {}
 };
 
-// Derivatives (Derivatives.hpp:54) on device arrays in the direction's
-// contiguous layout.
+// Derivatives (Derivatives.hpp:54) and Filter (Filter.hpp:31): the three
+// operators of one direction on an operator-only handle (cs3d_op_create), no
+// solver state.  calc1stDerivField / calc2ndDerivField / filterField take
+// host arrays in the direction's contiguous layout and return when the
+// result is there, as the reference's do (Derivatives.hpp:167-168,
+// Filter.hpp:115); the *_dev forms take device arrays and queue the work on
+// the handle's stream (stream()).
 class Derivatives_GB300 {
   public:
     enum Direct { DIRX = CS3D_DIRX, DIRY = CS3D_DIRY, DIRZ = CS3D_DIRZ };
-    cs3d_handle *h = nullptr;
+    cs3d_op *op = nullptr;
     Direct currentDir;
     Derivatives_GB300(Domain *dom, BC::BCType bcType, Direct dir, double alphaF = 0.49) : currentDir(dir) {
         cs3d_config c;
@@ -225,22 +235,27 @@ class Derivatives_GB300 {
         c.Lx = dom->Lx; c.Ly = dom->Ly; c.Lz = dom->Lz;
         c.bc_type[dir] = bcType;
         c.alphaF = alphaF;
-        c.mu_ref = 1.0;
-        c.CFL = 1.0;
-        c.filter_step = 1;
-        check(cs3d_create(&c, &h), "cs3d_create");
+        check(cs3d_op_create(&c, dir, &op), "cs3d_op_create");
     }
     Derivatives_GB300(const Derivatives_GB300 &) = delete;
     Derivatives_GB300 &operator=(const Derivatives_GB300 &) = delete;
-    virtual ~Derivatives_GB300() { cs3d_destroy(h); }
-    // synchronous, like the reference's calls
-    void calc1stDerivField(const double *in_dev, double *out_dev) {
-        check(cs3d_deriv1(h, currentDir, in_dev, out_dev), "cs3d_deriv1");
-        check(cs3d_sync(h), "cs3d_sync");
+    virtual ~Derivatives_GB300() { cs3d_op_destroy(op); }
+    void calc1stDerivField(const double *dataIn, double *dataOut) {
+        check(cs3d_op_apply_host(op, CS3D_OP_DERIV1, dataIn, dataOut), "calc1stDerivField");
     }
-    void calc2ndDerivField(const double *in_dev, double *out_dev) {
-        check(cs3d_deriv2(h, currentDir, in_dev, out_dev), "cs3d_deriv2");
-        check(cs3d_sync(h), "cs3d_sync");
+    void calc2ndDerivField(const double *dataIn, double *dataOut) {
+        check(cs3d_op_apply_host(op, CS3D_OP_DERIV2, dataIn, dataOut), "calc2ndDerivField");
+    }
+    void calc1stDerivField_dev(const double *in_dev, double *out_dev) {
+        check(cs3d_op_apply(op, CS3D_OP_DERIV1, in_dev, out_dev), "cs3d_op_apply");
+    }
+    void calc2ndDerivField_dev(const double *in_dev, double *out_dev) {
+        check(cs3d_op_apply(op, CS3D_OP_DERIV2, in_dev, out_dev), "cs3d_op_apply");
+    }
+    void *stream() {
+        void *s = nullptr;
+        check(cs3d_op_get_stream(op, &s), "cs3d_op_get_stream");
+        return s;
     }
 };
 
@@ -248,9 +263,11 @@ class Filter_GB300 : public Derivatives_GB300 {
   public:
     Filter_GB300(double alphaF, Domain *dom, BC::BCType bcType, Direct dir)
         : Derivatives_GB300(dom, bcType, dir, alphaF) {}
-    void filterField(const double *in_dev, double *out_dev) {
-        check(cs3d_filter(h, currentDir, in_dev, out_dev), "cs3d_filter");
-        check(cs3d_sync(h), "cs3d_sync");
+    void filterField(const double *dataIn, double *dataOut) {
+        check(cs3d_op_apply_host(op, CS3D_OP_FILTER, dataIn, dataOut), "filterField");
+    }
+    void filterField_dev(const double *in_dev, double *out_dev) {
+        check(cs3d_op_apply(op, CS3D_OP_FILTER, in_dev, out_dev), "cs3d_op_apply");
     }
 };
 

@@ -203,6 +203,30 @@ int cs3d_deriv1(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
 int cs3d_deriv2(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
 int cs3d_filter(cs3d_handle *h, int dir, const double *in_dev, double *out_dev);
 
+/* ---- operator-only handles ----------------------------------------------
+ * One direction's three compact operators with no solver state: replaces
+ * `new Derivatives(dom, bcType, dir)` (Derivatives.hpp:54-161) and
+ * `new Filter(alphaF, dom, bcType, dir)` (Filter.hpp:31-110), which build
+ * only the tridiagonal factors of their direction.  cs3d_op_create reads
+ * Nx, Ny, Nz, Lx, Ly, Lz, bc_type[dir] and alphaF from cfg; it allocates the
+ * operators' factors only (a few kB).  Fields are in the direction's
+ * contiguous layout (DIRX: XYZ, DIRY: YZX, DIRZ: ZXY, Macros.hpp:8-10).
+ *   cs3d_op_apply       device arrays, queued on the handle's stream
+ *                       (cs3d_op_get_stream); in and out must not overlap;
+ *   cs3d_op_apply_host  host arrays, synchronous, as the reference's
+ *                       calc1stDerivField(in, out) / filterField(in, out):
+ *                       the first call allocates 2*Nx*Ny*Nz doubles of device
+ *                       staging, kept until cs3d_op_destroy. */
+#define CS3D_OP_DERIV1 1  /* Derivatives::calc1stDerivField (Derivatives.cpp:3-49)  */
+#define CS3D_OP_DERIV2 2  /* Derivatives::calc2ndDerivField (Derivatives.cpp:51-96) */
+#define CS3D_OP_FILTER 3  /* Filter::filterField (Filter.cpp:129-171)               */
+typedef struct cs3d_op cs3d_op;
+int cs3d_op_create(const cs3d_config *cfg, int dir, cs3d_op **out);
+int cs3d_op_destroy(cs3d_op *op);
+int cs3d_op_apply(cs3d_op *op, int kind, const double *in_dev, double *out_dev);
+int cs3d_op_apply_host(cs3d_op *op, int kind, const double *in_host, double *out_host);
+int cs3d_op_get_stream(cs3d_op *op, void **stream);
+
 /* Kinetic energy and dissipation diagnostics of the Taylor-Green case,
  * the columns of calcTaylorGreenQuantities (CSolver_AWS.cpp:2175-2257):
  * out[0..6] = time, KEsum, dissSum, enstrophySum, enstrophy*2mu, meanMu,
@@ -310,7 +334,9 @@ int cs3d_rhs_vjp(cs3d_handle *h, const double *q, const double *lam, double *out
  * fixed static device array.  The arrays must be device memory of the
  * current device; the kernels run on `stream` (a cudaStream_t, NULL for the
  * default stream) and the call returns after the result is in *ke.
- * The first call on each device looks up the static array's address; make it
+ * Every call looks up the static array's address on the current device
+ * (cudaGetSymbolAddress), so a device reset between calls does no harm; the
+ * first call on a device may load the library's device code, so make it
  * before any stream capture starts.  Nothing has to be zeroed beforehand.
  * Two calls that overlap in time on one device share the array and race.
  * npts must be 1 .. 2^31-1 (CS3D_ERR_SHAPE otherwise). */

@@ -50,6 +50,24 @@ def test_config_validation_without_device(gpu_pkg):
     assert e.value.code == 1
 
 
+def test_operator_handle_validation_without_device(gpu_pkg):
+    """cs3d_op_create checks its direction's line length, L and BC type (and
+    nothing of the other directions) before looking for a device."""
+    cfg = gpu_pkg.make_config((16, 3, 2), (1.0, 1.0, 1.0))
+    for c, d, code in [(cfg.copy(Nx=6), 0, 2), (cfg.copy(Lx=0.0), 0, 1), (cfg, 3, 1)]:
+        with pytest.raises(gpu_pkg.CS3DError) as e:
+            gpu_pkg.Operator(c, d)
+        assert e.value.code == code, (e.value.code, str(e.value))
+    c = cfg.copy()
+    c.bc_type[0] = 4
+    with pytest.raises(gpu_pkg.CS3DError) as e:
+        gpu_pkg.Operator(c, 0)
+    assert e.value.code == 1
+    with pytest.raises(gpu_pkg.CS3DError) as e:
+        gpu_pkg.Operator(cfg, 1)  # Ny = 3: too short for the compact closures
+    assert e.value.code == 2
+
+
 def test_valid_config_reports_missing_device(gpu_pkg):
     import torch
     if torch.cuda.is_available():

@@ -85,3 +85,35 @@ def test_wall_closure_exact_on_cubic(gpu_pkg):
     f = 1 + 2 * x - x ** 2 + 0.5 * x ** 3
     out = _run(gpu_pkg, 1, 0, 1, (N, 2, 2), (L, 1.0, 1.0), 0.49, np.tile(f, (4, 1)))
     assert np.abs(out - (2 - 2 * x + 1.5 * x ** 2)[None, :]).max() < 1e-10
+
+
+def test_operator_handle_matches_reference_fixtures(gpu_pkg):
+    """The operator-only handle (cs3d_op_apply_host, host arrays as the
+    reference's calc1stDerivField / calc2ndDerivField / filterField take them,
+    and cs3d_op_apply on device arrays) on the exact grids of the reference
+    fixtures -- no widening of the other directions."""
+    import torch
+    g = load_golden("ref_lineops.npz")
+    L = tuple(float(v) for v in g["L"])
+    aF = float(g["alphaF"])
+    i = 0
+    while f"in{i}" in g:
+        kind, d, bc, nx, ny, nz = [int(v) for v in g[f"meta{i}"]]
+        bt = [gpu_pkg.PERIODIC_SOLVE] * 3
+        bt[d] = bc
+        cfg = gpu_pkg.make_config((nx, ny, nz), L, bc_type=tuple(bt), alphaF=aF)
+        op = gpu_pkg.Operator(cfg, d)
+        lines = np.asarray(g[f"in{i}"], dtype=np.float64).reshape(-1)
+        ref = np.asarray(g[f"out{i}"]).reshape(-1)
+        assert lines.size == nx * ny * nz
+        out = op.apply_host(kind, lines)
+        assert rel_err(out, ref) <= TOL, (i, kind, d, bc, rel_err(out, ref))
+        x = torch.from_numpy(lines).cuda()
+        y = torch.empty_like(x)
+        torch.cuda.synchronize()
+        op.apply(kind, x.data_ptr(), y.data_ptr())
+        torch.cuda.ExternalStream(op.stream()).synchronize()
+        assert np.array_equal(y.cpu().numpy(), out), i
+        op.close()
+        i += 1
+    assert i >= 20

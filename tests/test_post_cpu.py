@@ -1,10 +1,11 @@
 """The post-processor's vorticity and Q-criterion (PostProcess.cpp:190-310),
 restated in the oracle: against the analytic values of the Taylor-Green
-initial field.  The reference's post-processor is a stand-alone program with
-fixed input paths and a text reader that cannot read its own binary dumps, so
-it is pinned through its operators (the line operators, bit for bit in
-test_oracle_pin.py) and this known answer."""
+initial field, and against the reference's own post-processor run on its own
+512 x 256 x 128 grid (tests/golden/ref_postprocess.npz, made by
+tests/golden/make_postprocess_golden.py from the unmodified program)."""
 import numpy as np
+
+from conftest import load_golden
 
 
 def test_oracle_vorticity_q_taylor_green(oracle, cases):
@@ -25,3 +26,18 @@ def test_oracle_vorticity_q_taylor_green(oracle, cases):
     q_exact = 0.5 * (W ** 2).sum(axis=(0, 1)) - 0.5 * (S ** 2).sum(axis=(0, 1))
     assert np.abs(vort - np.sqrt((w ** 2).sum(axis=0))).max() <= 1e-5
     assert np.abs(q - q_exact).max() <= 1e-5 * np.abs(q_exact).max()
+
+
+def test_oracle_vorticity_q_matches_reference_postprocessor(oracle, cases):
+    """The restatement on the post-processor's grid and state: the same
+    numbers as the reference program's vortMag and qCrit, FP64 in full."""
+    g = load_golden("ref_postprocess.npz")
+    cfg, q = cases.postprocess_grid()
+    p = oracle.OraclePort(cfg)
+    for f, name in enumerate(("rho1", "rhoU1", "rhoV1", "rhoW1", "rhoE1")):
+        p.set(name, q[f])
+    vort, qc = p.vorticity_q()
+    idx = g["idx"]
+    ev = np.abs(vort.reshape(-1)[idx] - g["vort"]).max() / float(g["vort_max"])
+    eq = np.abs(qc.reshape(-1)[idx] - g["qcrit"]).max() / float(g["qcrit_max"])
+    assert ev <= 1e-14 and eq <= 1e-14, (ev, eq)
