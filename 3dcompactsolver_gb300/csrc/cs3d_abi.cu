@@ -338,6 +338,8 @@ struct cs3d_handle {
     DevOp<float> op32fc[3];  // FP32 filter correction F - I (mixed form)
     // tiles
     int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads[3] = {128, 128, 128};
+    int zpipe_grid = 0, zslot_bytes = 0;  // pipelined z sweep (mixed form): blocks, slot bytes (0: none)
+    int zpipe_on = 1;                     // CS3D_OPT_SWEEP_PIPELINE
     // step state
     int timeStep = 0, filterTimeStep = 0;
     int ic_done = 0;
@@ -644,6 +646,19 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
+    // The mixed form's z sweep runs pipelined where two slots of 8-line tiles
+    // fit in shared memory: one persistent 512-thread block per SM solves one
+    // tile while it consumes the previous one and loads the next.
+    if (h->mixed) {
+        const size_t slot = (sweep_smem_bytes(4, sweep_nbuf(2), 8, 8, Nd[2]) + 127) & ~(size_t)127;
+        int nsm = 0;
+        CS3D_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev));
+        const int ntiles = ((cfg->Nx + 7) / 8) * cfg->Ny;
+        if (2 * slot <= 220 * 1024 && nsm > 0) {
+            h->zslot_bytes = (int)slot;
+            h->zpipe_grid = ntiles < nsm ? ntiles : nsm;
+        }
+    }
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
     return CS3D_OK;
@@ -881,11 +896,14 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.sigma = h->sigma;
     a.savg = h->savg;
     for (int d = 0; d < 3; d++) {
-        a.threads = h->threads[d];
-        a.L = h->L[d];
-        a.lgL = ilog2(h->L[d]);
+        const bool zpipe = d == 2 && sizeof(T) == 4 && h->zpipe_grid > 0 && h->zpipe_on;
+        a.pipe_grid = zpipe ? h->zpipe_grid : 0;
+        a.slot_bytes = h->zslot_bytes;
+        a.threads = zpipe ? z_pipe_threads() : h->threads[d];
+        a.L = zpipe ? 8 : h->L[d];
+        a.lgL = ilog2(a.L);
         a.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
-        a.P = h->L[d] + (d == 0 ? 1 : 0);
+        a.P = a.L + (d == 0 ? 1 : 0);
         if (sizeof(T) == 8) {
             a.d1 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][0].op);
             a.d2 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][1].op);
@@ -1184,6 +1202,8 @@ extern "C" int cs3d_set_option(cs3d_handle *h, int option, int value) {
         h->store_diag = value != 0;
     } else if (option == CS3D_OPT_KERNEL_TIMING) {
         h->timing = value != 0;
+    } else if (option == CS3D_OPT_SWEEP_PIPELINE) {
+        h->zpipe_on = value != 0;
     } else {
         return fail(CS3D_ERR_ARG, "unknown option %d", option);
     }

@@ -256,218 +256,286 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZWY, ZWY, 0, ZRW, ZRW, 0}, {ZF1, ZF1, 0, ZF2, ZF2, 0},
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
+// The z sweep's three phases as functions of (tile, shared-memory slot,
+// thread range), so that the one-tile kernel (all threads run A, B, C in
+// turn) and the pipelined kernel (solver warps run B of one tile while the
+// other warps run C of the previous tile and A of the next) execute the same
+// per-point arithmetic in the same order: their results are identical.
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
-    const int L = a.L, P = PC > 0 ? PC : a.P;
-    const Tile t = make_tile<2>(a.g, L);
-    const int N = t.N, NL = N * L;
-    Smem<T> sm = smem_layout<T>(ZNB, L, P, N);
-    struct InA { Pt pt; T v[13]; };
-    batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
-        [&](InA &in, int p) {
-            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
-            const unsigned gi = in.pt.gi;
+struct ZSweep {
+    // A: stage the inputs of the 16 z-solves of tile t in sm
+    static __device__ __forceinline__ void load(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+                                                int nthr) {
+        const int L = a.L, P = PC > 0 ? PC : a.P;
+        const int NL = t.N * L;
+        struct InA { Pt pt; T v[13]; };
+        batched<InA, sizeof(T) == 4 ? 4 : 2>(NL, tid, nthr,
+            [&](InA &in, int p) {
+                in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+                const unsigned gi = in.pt.gi;
 #pragma unroll
-            for (int f = 0; f < 4; ++f) in.v[f] = a.qs[f + 1][gi];
+                for (int f = 0; f < 4; ++f) in.v[f] = a.qs[f + 1][gi];
 #pragma unroll
-            for (int f = 0; f < 5; ++f) in.v[4 + f] = a.prim[f][gi];
-            in.v[9] = a.dx[0][gi];
-            in.v[10] = a.dy[1][gi];
-            in.v[11] = a.dx[2][gi];
-            in.v[12] = a.dy[2][gi];
-        },
-        [&](InA &in) {
-            if (!in.pt.ok) return;
-            const int o = in.pt.o;
-            const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
-            const T W = in.v[6], pp = in.v[7];
-            sm.b(ZU)[o] = in.v[4];
-            sm.b(ZV)[o] = in.v[5];
-            sm.b(ZW)[o] = W;
-            sm.b(ZT)[o] = in.v[8];
-            sm.b(ZS)[o] = in.v[9] + in.v[10];
-            sm.b(ZWX)[o] = in.v[11];
-            sm.b(ZWY)[o] = in.v[12];
-            sm.b(ZRW)[o] = rw;
-            sm.b(ZF1)[o] = ru * W;
-            sm.b(ZF2)[o] = rv * W;
-            sm.b(ZF3)[o] = rw * W + pp;
-            sm.b(ZF4)[o] = re * W + W * pp;
-        });
-    __syncthreads();
-    run_tasks<T, 2, PC>(sm, kTasksZ, 8, L, t.nlines, a.d1, a.d2);
-    __syncthreads();
-    const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), c23 = T(2.0 / 3.0), cpPr = (T)a.gas.cpPr;
-    const double dt = *a.dt;
-    const T dtw = (T)dt;
-    const int st = a.rk_step;
-    const bool tvd = a.rk == 1;
-    // which state arrays the update reads (uniform over the launch):
-    //   qa = q1 (RK4 stage 1, all TVD-RK3 stages) or q2 (RK4 stages 2-4)
-    //   qb = q1 for the FP64 RK4 qk update on stages 2-3, or the FP64 qk of
-    //        TVD-RK3 stages 2-3
-    //   mixed RK4: q2 accumulates every stage's increment in FP64; the next
-    //   stage input qk = q1 + b dq exists only as an FP32 shadow, formed from
-    //   q1's shadow (the stage input itself on stage 1)
-    const bool use_q1a = tvd || st == 1;
-    const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
-    const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
-    const bool need_qs = a.mixed_rk4 && st == 1;
-    // Phase C runs in two passes over the same points, each point by the same
-    // thread in both (so no barrier between them): C1 forms the right-hand
-    // side and parks dq = dt*RHS in the point's own, now unused, solve slots;
-    // C2 streams the FP64 state through the RK update.  Each pass keeps fewer
-    // values live than one fused pass, so more points' loads are in flight.
-    constexpr int kDq[5] = {ZS, ZWX, ZWY, ZRW, ZF1};
-    struct InC1 {
-        Pt pt;
-        T v[18];
-        T qsv[5];
-    };
-    pipelined<InC1>(NL,
-        [&](InC1 &in, int p) {
-            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
-            const unsigned gi = in.pt.gi;
-            in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi];
-            in.v[3] = a.mu[gi]; in.v[4] = a.amu[gi];
+                for (int f = 0; f < 5; ++f) in.v[4 + f] = a.prim[f][gi];
+                in.v[9] = a.dx[0][gi];
+                in.v[10] = a.dy[1][gi];
+                in.v[11] = a.dx[2][gi];
+                in.v[12] = a.dy[2][gi];
+            },
+            [&](InA &in) {
+                if (!in.pt.ok) return;
+                const int o = in.pt.o;
+                const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
+                const T W = in.v[6], pp = in.v[7];
+                sm.b(ZU)[o] = in.v[4];
+                sm.b(ZV)[o] = in.v[5];
+                sm.b(ZW)[o] = W;
+                sm.b(ZT)[o] = in.v[8];
+                sm.b(ZS)[o] = in.v[9] + in.v[10];
+                sm.b(ZWX)[o] = in.v[11];
+                sm.b(ZWY)[o] = in.v[12];
+                sm.b(ZRW)[o] = rw;
+                sm.b(ZF1)[o] = ru * W;
+                sm.b(ZF2)[o] = rv * W;
+                sm.b(ZF3)[o] = rw * W + pp;
+                sm.b(ZF4)[o] = re * W + W * pp;
+            });
+    }
+    // B: the 16 solves (8 pairs) of every line of the tile
+    static __device__ __forceinline__ void solve(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+                                                 int nthr) {
+        run_tasks<T, 2, PC>(sm, kTasksZ, 8, a.L, t.nlines, a.d1, a.d2, tid, nthr);
+    }
+    // C: right-hand side, dq and the RK update of every point of the tile
+    static __device__ __forceinline__ void consume(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+                                                   int nthr) {
+        const int L = a.L, P = PC > 0 ? PC : a.P;
+        const int NL = t.N * L;
+        const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), c23 = T(2.0 / 3.0), cpPr = (T)a.gas.cpPr;
+        const double dt = *a.dt;
+        const T dtw = (T)dt;
+        const int st = a.rk_step;
+        const bool tvd = a.rk == 1;
+        // which state arrays the update reads (uniform over the launch):
+        //   qa = q1 (RK4 stage 1, all TVD-RK3 stages) or q2 (RK4 stages 2-4)
+        //   qb = q1 for the FP64 RK4 qk update on stages 2-3, or the FP64 qk of
+        //        TVD-RK3 stages 2-3
+        //   mixed RK4: q2 accumulates every stage's increment in FP64; the next
+        //   stage input qk = q1 + b dq exists only as an FP32 shadow, formed from
+        //   q1's shadow (the stage input itself on stage 1)
+        const bool use_q1a = tvd || st == 1;
+        const bool need_qb = (!tvd && !a.mixed_rk4 && st > 1 && st < 4) || (tvd && st > 1);
+        const bool need_q1s = a.mixed_rk4 && st > 1 && st < 4;
+        const bool need_qs = a.mixed_rk4 && st == 1;
+        // Phase C runs in two passes over the same points, each point by the same
+        // thread in both (so no barrier between them): C1 forms the right-hand
+        // side and parks dq = dt*RHS in the point's own, now unused, solve slots;
+        // C2 streams the FP64 state through the RK update.  Each pass keeps fewer
+        // values live than one fused pass, so more points' loads are in flight.
+        constexpr int kDq[5] = {ZS, ZWX, ZWY, ZRW, ZF1};
+        struct InC1 {
+            Pt pt;
+            T v[18];
+            T qsv[5];
+        };
+        pipelined<InC1>(NL, tid, nthr,
+            [&](InC1 &in, int p) {
+                in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+                const unsigned gi = in.pt.gi;
+                in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi];
+                in.v[3] = a.mu[gi]; in.v[4] = a.amu[gi];
 #pragma unroll
-            for (int f = 0; f < 4; ++f) { in.v[5 + f] = a.dx[f][gi]; in.v[9 + f] = a.dy[f][gi]; }
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                in.v[13 + f] = a.R[f][gi];
-                in.qsv[f] = a.sponge ? a.qs[f][gi] : T(0);
-            }
-        },
-        [&](InC1 &in) {
-            if (!in.pt.ok) return;
-            const Pt &p = in.pt;
-            const unsigned gi = p.gi;
-            const Zn<T> zz = zn(a.d1, a.d2, p.n);
-            const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3], amu = in.v[4];
-            const T Ux = in.v[5], Vx = in.v[6], Wx = in.v[7], Tx = in.v[8];
-            const T Uy = in.v[9], Vy = in.v[10], Wy = in.v[11], Ty = in.v[12];
-            const T Uz = gz(sm, ZU, p, L, zz.z1), Uzz = gz(sm, ZU2, p, L, zz.z2);
-            const T Vz = gz(sm, ZV, p, L, zz.z1), Vzz = gz(sm, ZV2, p, L, zz.z2);
-            const T Wz = gz(sm, ZW, p, L, zz.z1), Wzz = gz(sm, ZW2, p, L, zz.z2);
-            const T Tz = gz(sm, ZT, p, L, zz.z1), Tzz = gz(sm, ZT2, p, L, zz.z2);
-            const T S = gz(sm, ZS, p, L, zz.z1);  // Uxz + Vyz
-            const T Wxz = gz(sm, ZWX, p, L, zz.z1), Wyz = gz(sm, ZWY, p, L, zz.z1);
-            const T cez = gz(sm, ZRW, p, L, zz.z1);
-            const T f1 = gz(sm, ZF1, p, L, zz.z1), f2 = gz(sm, ZF2, p, L, zz.z1);
-            const T f3 = gz(sm, ZF3, p, L, zz.z1), f4 = gz(sm, ZF4, p, L, zz.z1);
-            T src[5] = {T(0), T(0), T(0), T(0), T(0)};
-            if (a.sponge) {  // sigma (avg - q), SpongeBC / CSolver_AWS.hpp:228
-                const T sg = to_work<T>(a.sigma[gi]);
-#pragma unroll
-                for (int f = 0; f < 5; ++f) src[f] = sg * (to_work<T>(a.savg.f[f][gi]) - in.qsv[f]);
-            }
-            const T MuX = amu * Tx, MuY = amu * Ty, MuZ = amu * Tz;
-            T R[5];
-            R[0] = in.v[13];
-            R[1] = in.v[14] + mu * (Uzz + c13 * Wxz) - f1 + c43 * MuX * (Ux - T(0.5) * Vy - T(0.5) * Wz) +
-                   MuY * (Uy + Vx) + MuZ * (Wx + Uz) + src[1];
-            R[2] = in.v[15] + mu * (Vzz + c13 * Wyz) - f2 + c43 * MuY * (Vy - T(0.5) * Ux - T(0.5) * Wz) +
-                   MuX * (Uy + Vx) + MuZ * (Wy + Vz) + src[2];
-            R[3] = in.v[16] + mu * (c43 * Wzz + c13 * S) - f3 + c43 * MuZ * (Wz - T(0.5) * Ux - T(0.5) * Vy) +
-                   MuX * (Wx + Uz) + MuY * (Wy + Vz) + src[3];
-            const T q2s = Ux * Ux + Vy * Vy + Wz * Wz;
-            const T sq = Uy * Uy + Uz * Uz + Vx * Vx + Vz * Vz + Wx * Wx + Wy * Wy;
-            const T cr = Ux * Vy + Ux * Wz + Vy * Wz;
-            const T sh = Uy * Vx + Uz * Wx + Vz * Wy;
-            const T v1 = mu * (U * Uzz + V * Vzz + W * (c43 * Wzz) + c13 * (U * Wxz + V * Wyz + W * S) + c43 * q2s +
-                               sq - c43 * cr + T(2.0) * sh);
-            const T v2 = c43 * (U * MuX * Ux + V * MuY * Vy + W * MuZ * Wz) - c23 * U * MuX * (Vy + Wz) -
-                         c23 * V * MuY * (Ux + Wz) - c23 * W * MuZ * (Ux + Vy) + U * MuY * (Uy + Vx) +
-                         U * MuZ * (Uz + Wx) + V * MuX * (Uy + Vx) + V * MuZ * (Vz + Wy) + W * MuX * (Uz + Wx) +
-                         W * MuY * (Vz + Wy);
-            R[4] = in.v[17] + cpPr * (MuX * Tx + MuY * Ty + MuZ * Tz + mu * Tzz) + v1 + v2 - f4 + T(2.0) * src[4];
-            // continuity and the post-step boundary fix-up (CSolver_AWS.cpp:1506-1679)
-            int i, j, k;
-            coords<2>(t, p.l, p.n, i, j, k);
-            const int fc = faces_of(a.g, i, j, k);
-            const int wd = a.wall_faces ? wall_dir(fc & a.wall_faces) : -1;
-            if (wd == 2) R[0] = -cez;
-            else if (wd < 0) R[0] = R[0] - cez + src[0];
-            const bool zero_all = (fc & a.sponge_kind_faces) != 0;
-            const bool zero_mom = wd >= 0;
-            if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
-                a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
-            }
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                // plain form: dq = dt * RHS in FP64; mixed form: in FP32
-                T d = sizeof(T) == 8 ? (T)(dt * (double)R[f]) : dtw * R[f];
-                if (zero_all || (f > 0 && zero_mom)) d = T(0);
-                if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
-                sm.b(kDq[f])[p.o] = d;
-            }
-        });
-    struct InC2 {
-        Pt pt;
-        double qa[5], qb[5];
-        T qsv[5];    // q1's shadow: the stage input qs on stage 1, q1s on 2-3
-    };
-    batched<InC2, CS3D_ZC2>(NL,
-        [&](InC2 &in, int p) {
-            in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
-            const unsigned gi = in.pt.gi;
-#pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
-                in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
-                in.qsv[f] = need_qs ? a.qs[f][gi] : need_q1s ? (T)a.q1s[f][gi] : T(0);
-            }
-        },
-        [&](InC2 &in) {
-            if (!in.pt.ok) return;
-            const unsigned gi = in.pt.gi;
-            if (sizeof(T) == 8) {
-                // plain form: the reference's RK update in FP64
+                for (int f = 0; f < 4; ++f) { in.v[5 + f] = a.dx[f][gi]; in.v[9 + f] = a.dy[f][gi]; }
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    const double d = (double)sm.b(kDq[f])[in.pt.o];
-                    if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
-                        if (st == 1) a.qk.f[f][gi] = in.qa[f] + d;
-                        else if (st == 2) a.qk.f[f][gi] = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * d;
-                        else a.q2.f[f][gi] = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * d;
-                    } else {    // RK4 (RK4.hpp:35-118); qa = q1 (stage 1) or q2
-                        const double ca = (st == 1 || st == 4) ? (1.0 / 6.0) : (1.0 / 3.0);
-                        const double cb = (st == 3) ? 1.0 : 0.5;
-                        a.q2.f[f][gi] = in.qa[f] + ca * d;
-                        if (st == 1) a.qk.f[f][gi] = in.qa[f] + cb * d;
-                        else if (st < 4) a.qk.f[f][gi] = in.qb[f] + cb * d;
-                    }
+                    in.v[13 + f] = a.R[f][gi];
+                    in.qsv[f] = a.sponge ? a.qs[f][gi] : T(0);
                 }
-            } else {
-                // mixed form: the FP32 increment accumulated into the FP64 state
+            },
+            [&](InC1 &in) {
+                if (!in.pt.ok) return;
+                const Pt &p = in.pt;
+                const unsigned gi = p.gi;
+                const Zn<T> zz = zn(a.d1, a.d2, p.n);
+                const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3], amu = in.v[4];
+                const T Ux = in.v[5], Vx = in.v[6], Wx = in.v[7], Tx = in.v[8];
+                const T Uy = in.v[9], Vy = in.v[10], Wy = in.v[11], Ty = in.v[12];
+                const T Uz = gz(sm, ZU, p, L, zz.z1), Uzz = gz(sm, ZU2, p, L, zz.z2);
+                const T Vz = gz(sm, ZV, p, L, zz.z1), Vzz = gz(sm, ZV2, p, L, zz.z2);
+                const T Wz = gz(sm, ZW, p, L, zz.z1), Wzz = gz(sm, ZW2, p, L, zz.z2);
+                const T Tz = gz(sm, ZT, p, L, zz.z1), Tzz = gz(sm, ZT2, p, L, zz.z2);
+                const T S = gz(sm, ZS, p, L, zz.z1);  // Uxz + Vyz
+                const T Wxz = gz(sm, ZWX, p, L, zz.z1), Wyz = gz(sm, ZWY, p, L, zz.z1);
+                const T cez = gz(sm, ZRW, p, L, zz.z1);
+                const T f1 = gz(sm, ZF1, p, L, zz.z1), f2 = gz(sm, ZF2, p, L, zz.z1);
+                const T f3 = gz(sm, ZF3, p, L, zz.z1), f4 = gz(sm, ZF4, p, L, zz.z1);
+                T src[5] = {T(0), T(0), T(0), T(0), T(0)};
+                if (a.sponge) {  // sigma (avg - q), SpongeBC / CSolver_AWS.hpp:228
+                    const T sg = to_work<T>(a.sigma[gi]);
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) src[f] = sg * (to_work<T>(a.savg.f[f][gi]) - in.qsv[f]);
+                }
+                const T MuX = amu * Tx, MuY = amu * Ty, MuZ = amu * Tz;
+                T R[5];
+                R[0] = in.v[13];
+                R[1] = in.v[14] + mu * (Uzz + c13 * Wxz) - f1 + c43 * MuX * (Ux - T(0.5) * Vy - T(0.5) * Wz) +
+                       MuY * (Uy + Vx) + MuZ * (Wx + Uz) + src[1];
+                R[2] = in.v[15] + mu * (Vzz + c13 * Wyz) - f2 + c43 * MuY * (Vy - T(0.5) * Ux - T(0.5) * Wz) +
+                       MuX * (Uy + Vx) + MuZ * (Wy + Vz) + src[2];
+                R[3] = in.v[16] + mu * (c43 * Wzz + c13 * S) - f3 + c43 * MuZ * (Wz - T(0.5) * Ux - T(0.5) * Vy) +
+                       MuX * (Wx + Uz) + MuY * (Wy + Vz) + src[3];
+                const T q2s = Ux * Ux + Vy * Vy + Wz * Wz;
+                const T sq = Uy * Uy + Uz * Uz + Vx * Vx + Vz * Vz + Wx * Wx + Wy * Wy;
+                const T cr = Ux * Vy + Ux * Wz + Vy * Wz;
+                const T sh = Uy * Vx + Uz * Wx + Vz * Wy;
+                const T v1 = mu * (U * Uzz + V * Vzz + W * (c43 * Wzz) + c13 * (U * Wxz + V * Wyz + W * S) + c43 * q2s +
+                                   sq - c43 * cr + T(2.0) * sh);
+                const T v2 = c43 * (U * MuX * Ux + V * MuY * Vy + W * MuZ * Wz) - c23 * U * MuX * (Vy + Wz) -
+                             c23 * V * MuY * (Ux + Wz) - c23 * W * MuZ * (Ux + Vy) + U * MuY * (Uy + Vx) +
+                             U * MuZ * (Uz + Wx) + V * MuX * (Uy + Vx) + V * MuZ * (Vz + Wy) + W * MuX * (Uz + Wx) +
+                             W * MuY * (Vz + Wy);
+                R[4] = in.v[17] + cpPr * (MuX * Tx + MuY * Ty + MuZ * Tz + mu * Tzz) + v1 + v2 - f4 + T(2.0) * src[4];
+                // continuity and the post-step boundary fix-up (CSolver_AWS.cpp:1506-1679)
+                int i, j, k;
+                coords<2>(t, p.l, p.n, i, j, k);
+                const int fc = faces_of(a.g, i, j, k);
+                const int wd = a.wall_faces ? wall_dir(fc & a.wall_faces) : -1;
+                if (wd == 2) R[0] = -cez;
+                else if (wd < 0) R[0] = R[0] - cez + src[0];
+                const bool zero_all = (fc & a.sponge_kind_faces) != 0;
+                const bool zero_mom = wd >= 0;
+                if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
+                    a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
+                }
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
-                    const T d = sm.b(kDq[f])[in.pt.o];
-                    if (tvd) {
-                        const double dd = to_f64(d);
-                        double nv;
-                        if (st == 1) { nv = in.qa[f] + dd; a.qk.f[f][gi] = nv; }
-                        else if (st == 2) { nv = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * dd; a.qk.f[f][gi] = nv; }
-                        else { nv = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
-                        if (a.shadow_target != SHADOW_NONE) a.shadow_out[f][gi] = narrow(nv);
-                    } else {
-                        // RK4: q2 += a_s dq in FP64 on every stage (RK4.hpp:35-118)
-                        const T ca = (st == 1 || st == 4) ? T(1.0 / 6.0) : T(1.0 / 3.0);
-                        const T cb = (st == 3) ? T(1.0) : T(0.5);
-                        const double q2n = in.qa[f] + to_f64(ca * d);
-                        a.q2.f[f][gi] = q2n;
-                        if (st < 4) {
-                            // the next stage input qk = q1 + cb*dq, kept as an FP32 shadow
-                            a.shadow_out[f][gi] = fma(cb, d, in.qsv[f]);
+                    // plain form: dq = dt * RHS in FP64; mixed form: in FP32
+                    T d = sizeof(T) == 8 ? (T)(dt * (double)R[f]) : dtw * R[f];
+                    if (zero_all || (f > 0 && zero_mom)) d = T(0);
+                    if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
+                    sm.b(kDq[f])[p.o] = d;
+                }
+            });
+        struct InC2 {
+            Pt pt;
+            double qa[5], qb[5];
+            T qsv[5];    // q1's shadow: the stage input qs on stage 1, q1s on 2-3
+        };
+        batched<InC2, CS3D_ZC2>(NL, tid, nthr,
+            [&](InC2 &in, int p) {
+                in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
+                const unsigned gi = in.pt.gi;
+#pragma unroll
+                for (int f = 0; f < 5; ++f) {
+                    in.qa[f] = use_q1a ? a.q1.f[f][gi] : a.q2.f[f][gi];
+                    in.qb[f] = need_qb ? (tvd ? a.qk.f[f][gi] : a.q1.f[f][gi]) : 0.0;
+                    in.qsv[f] = need_qs ? a.qs[f][gi] : need_q1s ? (T)a.q1s[f][gi] : T(0);
+                }
+            },
+            [&](InC2 &in) {
+                if (!in.pt.ok) return;
+                const unsigned gi = in.pt.gi;
+                if (sizeof(T) == 8) {
+                    // plain form: the reference's RK update in FP64
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        const double d = (double)sm.b(kDq[f])[in.pt.o];
+                        if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
+                            if (st == 1) a.qk.f[f][gi] = in.qa[f] + d;
+                            else if (st == 2) a.qk.f[f][gi] = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * d;
+                            else a.q2.f[f][gi] = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * d;
+                        } else {    // RK4 (RK4.hpp:35-118); qa = q1 (stage 1) or q2
+                            const double ca = (st == 1 || st == 4) ? (1.0 / 6.0) : (1.0 / 3.0);
+                            const double cb = (st == 3) ? 1.0 : 0.5;
+                            a.q2.f[f][gi] = in.qa[f] + ca * d;
+                            if (st == 1) a.qk.f[f][gi] = in.qa[f] + cb * d;
+                            else if (st < 4) a.qk.f[f][gi] = in.qb[f] + cb * d;
+                        }
+                    }
+                } else {
+                    // mixed form: the FP32 increment accumulated into the FP64 state
+#pragma unroll
+                    for (int f = 0; f < 5; ++f) {
+                        const T d = sm.b(kDq[f])[in.pt.o];
+                        if (tvd) {
+                            const double dd = to_f64(d);
+                            double nv;
+                            if (st == 1) { nv = in.qa[f] + dd; a.qk.f[f][gi] = nv; }
+                            else if (st == 2) { nv = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * dd; a.qk.f[f][gi] = nv; }
+                            else { nv = (1.0 / 3.0) * in.qa[f] + (2.0 / 3.0) * in.qb[f] + (2.0 / 3.0) * dd; a.q2.f[f][gi] = nv; }
+                            if (a.shadow_target != SHADOW_NONE) a.shadow_out[f][gi] = narrow(nv);
                         } else {
-                            if (a.shadow_target == SHADOW_Q2) a.shadow_out[f][gi] = narrow(q2n);
-                            // the filter's first pass input, q2 - fref in FP32
-                            if (a.fluct_out) a.fluct[f][gi] = narrow(q2n - a.fref[f]);
+                            // RK4: q2 += a_s dq in FP64 on every stage (RK4.hpp:35-118)
+                            const T ca = (st == 1 || st == 4) ? T(1.0 / 6.0) : T(1.0 / 3.0);
+                            const T cb = (st == 3) ? T(1.0) : T(0.5);
+                            const double q2n = in.qa[f] + to_f64(ca * d);
+                            a.q2.f[f][gi] = q2n;
+                            if (st < 4) {
+                                // the next stage input qk = q1 + cb*dq, kept as an FP32 shadow
+                                a.shadow_out[f][gi] = fma(cb, d, in.qsv[f]);
+                            } else {
+                                if (a.shadow_target == SHADOW_Q2) a.shadow_out[f][gi] = narrow(q2n);
+                                // the filter's first pass input, q2 - fref in FP32
+                                if (a.fluct_out) a.fluct[f][gi] = narrow(q2n - a.fref[f]);
+                            }
                         }
                     }
                 }
+            });
+    }
+};
+
+template <typename T, int PC>
+__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
+    const Tile t = make_tile<2>(a.g, a.L);
+    const Smem<T> sm = smem_layout<T>(ZNB, a.L, PC > 0 ? PC : a.P, t.N);
+    ZSweep<T, PC>::load(a, t, sm, threadIdx.x, blockDim.x);
+    __syncthreads();
+    ZSweep<T, PC>::solve(a, t, sm, threadIdx.x, blockDim.x);
+    __syncthreads();
+    ZSweep<T, PC>::consume(a, t, sm, threadIdx.x, blockDim.x);
+}
+
+// The pipelined z sweep (FP32-mixed form): one persistent block per SM walks
+// the tiles b, b + G, b + 2G, ... (G = gridDim.x) with two shared-memory
+// slots.  In iteration k the first kZSolveWarps warps solve tile k (slot
+// k & 1) while the other warps consume tile k - 1 and then load tile k + 1
+// into the slot tile k - 1 leaves (a barrier among those warps separates the
+// two), so the solve phase, which touches no global memory, runs while the
+// other warps stream.  One block barrier per iteration hands the slots over.
+constexpr int kZSolveWarps = 2;
+constexpr int kZPipeThreads = 512;
+
+template <int PC>
+__global__ void __launch_bounds__(kZPipeThreads, 1) k_sweep_z_pipe(SweepArgs<float> a) {
+    using Z = ZSweep<float, PC>;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
+    const int nxb = (a.g.Nx + L - 1) / L, ntiles = nxb * a.g.Ny;
+    const int G = gridDim.x, b = blockIdx.x;
+    const Smem<float> s0 = smem_layout<float>(ZNB, L, P, a.g.Nz);
+    const Smem<float> s1 = smem_layout_at<float>(smem_raw + a.slot_bytes, ZNB, L, P, a.g.Nz);
+    const int nsolve = 32 * kZSolveWarps;
+    const bool solver = (int)threadIdx.x < nsolve;
+    const int mtid = (int)threadIdx.x - nsolve, mthr = (int)blockDim.x - nsolve;
+    auto tile = [&](int tt) { return make_tile_at<2>(a.g, L, tt % nxb, tt / nxb); };
+    if (!solver && b < ntiles) Z::load(a, tile(b), s0, mtid, mthr);
+    __syncthreads();
+    for (int k = 0;; ++k) {
+        const int tk = b + k * G;  // solved in this iteration
+        if (tk - G >= ntiles) break;
+        const Smem<float> &cur = (k & 1) ? s1 : s0;
+        const Smem<float> &oth = (k & 1) ? s0 : s1;
+        if (solver) {
+            if (tk < ntiles) Z::solve(a, tile(tk), cur, threadIdx.x, nsolve);
+        } else {
+            if (k > 0) Z::consume(a, tile(tk - G), oth, mtid, mthr);
+            if (tk + G < ntiles) {
+                asm volatile("bar.sync 1, %0;" ::"r"(mthr) : "memory");
+                Z::load(a, tile(tk + G), oth, mtid, mthr);
             }
-        });
+        }
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -603,6 +671,8 @@ static size_t tile_smem(int nbuf, int L, int P, int N) {
     return sizeof(T) * ((size_t)nf + (size_t)nbuf * buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4)));
 }
 
+int z_pipe_threads() { return kZPipeThreads; }
+
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
     return prec_bytes == 8 ? tile_smem<double>(nbuf, L, P, N) : tile_smem<float>(nbuf, L, P, N);
 }
@@ -630,6 +700,13 @@ cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s) {
     const size_t sm = tile_smem<T>(sweep_nbuf(dir), a.L, a.P, N);
     const dim3 grid = tile_grid(dir, a.g, a.L);
     if constexpr (sizeof(T) == 4) {
+        if (dir == 2 && a.pipe_grid > 0 && a.P == 8) {
+            cudaError_t e = cudaFuncSetAttribute(k_sweep_z_pipe<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 2 * a.slot_bytes);
+            if (e != cudaSuccess) return e;
+            k_sweep_z_pipe<8><<<a.pipe_grid, kZPipeThreads, 2 * a.slot_bytes, s>>>(a);
+            return cudaGetLastError();
+        }
         if (dir == 0 && a.P == 9) return launch_tile_kernel(k_sweep_x<T, 9>, a, grid, sm, s);
         if (dir == 0 && a.P == 5) return launch_tile_kernel(k_sweep_x<T, 5>, a, grid, sm, s);
         if (dir == 1 && a.P == 16) return launch_tile_kernel(k_sweep_y<T, 16>, a, grid, sm, s);

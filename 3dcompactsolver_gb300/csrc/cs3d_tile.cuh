@@ -384,26 +384,29 @@ struct Tile {
     int ci, cj, ck;   // coordinates of (line 0, position 0)
 };
 
+// The tile of block coordinates (bx, by): bx counts tiles across the lines'
+// transverse direction (rows j for x-lines, columns i otherwise), by the
+// plane (k for x- and y-lines, row j for z-lines).
 template <int DIR>
-__device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
+__device__ __forceinline__ Tile make_tile_at(const Geom &g, int L, int bx, int by) {
     Tile t;
     const unsigned nxy = (unsigned)g.Nx * (unsigned)g.Ny;
     if (DIR == 0) {  // x-lines at rows j0.., plane k
-        int j0 = blockIdx.x * L, k = blockIdx.y;
+        int j0 = bx * L, k = by;
         t.base = (unsigned)k * nxy + (unsigned)j0 * g.Nx;
         t.sl = g.Nx; t.sn = 1;
         t.nlines = min(L, g.Ny - j0);
         t.N = g.Nx;
         t.ci = 0; t.cj = j0; t.ck = k;
     } else if (DIR == 1) {  // y-lines at columns i0.., plane k
-        int i0 = blockIdx.x * L, k = blockIdx.y;
+        int i0 = bx * L, k = by;
         t.base = (unsigned)k * nxy + i0;
         t.sl = 1; t.sn = g.Nx;
         t.nlines = min(L, g.Nx - i0);
         t.N = g.Ny;
         t.ci = i0; t.cj = 0; t.ck = k;
     } else {  // z-lines at columns i0.., row j
-        int i0 = blockIdx.x * L, j = blockIdx.y;
+        int i0 = bx * L, j = by;
         t.base = (unsigned)j * g.Nx + i0;
         t.sl = 1; t.sn = nxy;
         t.nlines = min(L, g.Nx - i0);
@@ -411,6 +414,11 @@ __device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
         t.ci = i0; t.cj = j; t.ck = 0;
     }
     return t;
+}
+
+template <int DIR>
+__device__ __forceinline__ Tile make_tile(const Geom &g, int L) {
+    return make_tile_at<DIR>(g, L, blockIdx.x, blockIdx.y);
 }
 
 // Point p of a tile: consecutive threads touch consecutive global addresses
@@ -472,15 +480,21 @@ __host__ __device__ inline int buf_stride(int N, int P, int L, int e) {
 }
 
 template <typename T>
-__device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ Smem<T> smem_layout_at(unsigned char *base, int nbuf, int L, int P, int N) {
     Smem<T> s;
     s.P = P;
     s.bstride = buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4));
-    s.fact = reinterpret_cast<T *>(smem_raw);
+    s.fact = reinterpret_cast<T *>(base);
     const int nf = (nbuf * L + 3) & ~3;
-    s.buf = reinterpret_cast<T *>(smem_raw) + nf;
+    s.buf = reinterpret_cast<T *>(base) + nf;
     return s;
+}
+
+extern __shared__ __align__(16) unsigned char smem_raw[];
+
+template <typename T>
+__device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
+    return smem_layout_at<T>(smem_raw, nbuf, L, P, N);
 }
 
 // Right-hand sides of nf line solves per line, computed by every thread of
@@ -521,18 +535,19 @@ __device__ __forceinline__ void rhs_pass(const Smem<T> &sm, int src0, int dst0, 
 // global loads of the thread's next point are issued before the current
 // point is computed, so memory latency overlaps the arithmetic.
 // ld(S&, p) loads point p; cp(S&) computes and stores it.
+// tid / nthr: this thread's index among the nthr threads sharing the loop.
 template <typename S, typename LD, typename CP>
-__device__ __forceinline__ void pipelined(int NL, LD &&ld, CP &&cp) {
-    int p = threadIdx.x;
+__device__ __forceinline__ void pipelined(int NL, int tid, int nthr, LD &&ld, CP &&cp) {
+    int p = tid;
     if (p >= NL) return;
     S s0, s1;
     ld(s0, p);
     for (;;) {
-        const int p1 = p + blockDim.x;
+        const int p1 = p + nthr;
         if (p1 < NL) ld(s1, p1);
         cp(s0);
         if (p1 >= NL) break;
-        const int p2 = p1 + blockDim.x;
+        const int p2 = p1 + nthr;
         if (p2 < NL) ld(s0, p2);
         cp(s1);
         if (p2 >= NL) break;
@@ -543,18 +558,22 @@ __device__ __forceinline__ void pipelined(int NL, LD &&ld, CP &&cp) {
 // Per-thread loop over the points of a tile in batches of B: the loads of B
 // points are issued together, then the B points are computed and stored.
 template <typename S, int B, typename LD, typename CP>
-__device__ __forceinline__ void batched(int NL, LD &&ld, CP &&cp) {
-    for (int p0 = threadIdx.x; p0 < NL; p0 += B * blockDim.x) {
+__device__ __forceinline__ void batched(int NL, int tid, int nthr, LD &&ld, CP &&cp) {
+    for (int p0 = tid; p0 < NL; p0 += B * nthr) {
         S s[B];
 #pragma unroll
         for (int b = 0; b < B; ++b) {
-            const int p = p0 + b * blockDim.x;
+            const int p = p0 + b * nthr;
             ld(s[b], p < NL ? p : p0);
             if (p >= NL) s[b].pt.ok = false;
         }
 #pragma unroll
         for (int b = 0; b < B; ++b) cp(s[b]);
     }
+}
+template <typename S, int B, typename LD, typename CP>
+__device__ __forceinline__ void batched(int NL, LD &&ld, CP &&cp) {
+    batched<S, B>(NL, (int)threadIdx.x, (int)blockDim.x, ld, cp);
 }
 
 // A task: solve A (src a, dst da, operator oa) and solve B, run together.
@@ -566,8 +585,8 @@ struct Task {
 // PC > 0: the caller has checked that the buffer pitch sm.P equals PC.
 template <typename T, int H, int PC = 0>
 __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
-                                          const LineOp<T> &op0, const LineOp<T> &op1) {
-    for (int w = threadIdx.x; w < ntask * L; w += blockDim.x) {
+                                          const LineOp<T> &op0, const LineOp<T> &op1, int tid, int nthr) {
+    for (int w = tid; w < ntask * L; w += nthr) {
         const int t = w / L, l = w - t * L;
         if (l >= nlines) continue;
         const Task tk = tasks[t];
@@ -576,6 +595,11 @@ __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, 
         solve_pair<T, H, PC>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
                              sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
     }
+}
+template <typename T, int H, int PC = 0>
+__device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
+                                          const LineOp<T> &op0, const LineOp<T> &op1) {
+    run_tasks<T, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, (int)threadIdx.x, (int)blockDim.x);
 }
 
 template <typename T>
