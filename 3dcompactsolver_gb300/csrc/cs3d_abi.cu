@@ -338,8 +338,6 @@ struct cs3d_handle {
     DevOp<float> op32fc[3];  // FP32 filter correction F - I (mixed form)
     // tiles
     int L[3] = {1, 1, 1}, Lf[3] = {1, 1, 1}, threads[3] = {128, 128, 128};
-    int zpipe_grid = 0, zslot_bytes = 0;  // pipelined z sweep (mixed form): blocks, slot bytes (0: none)
-    int zpipe_on = 1;                     // CS3D_OPT_SWEEP_PIPELINE
     // step state
     int timeStep = 0, filterTimeStep = 0;
     int ic_done = 0;
@@ -497,10 +495,15 @@ static int check_config(const cs3d_config *c) {
 // y and z sweeps of the mixed form at N = 128 this gives 8 lines: every
 // global access is then a full 32-byte sector, which measured faster than
 // narrower tiles with more blocks per SM.
-static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, int budget_kb = 72) {
+// sweep: the sweeps' tile layout (pair-interleaved in FP32), else planar.
+static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, int budget_kb = 72, bool sweep = false) {
     const size_t budget = (size_t)budget_kb * 1024;
     int L = 32;
-    while (L > 1 && sweep_smem_bytes((int)tb, nbuf, L, L + pitch_plus, N) > budget) L /= 2;
+    auto bytes = [&](int l) {
+        return sweep ? sweep_smem_bytes((int)tb, nbuf, l, l + pitch_plus, N)
+                     : planar_smem_bytes((int)tb, nbuf, l, l + pitch_plus, N);
+    };
+    while (L > 1 && bytes(L) > budget) L /= 2;
     return L;
 }
 
@@ -624,17 +627,18 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             if (r) return fail_free(r);
         }
     for (int d = 0; d < 3; d++) {
-        // Tile shape.  Default: the widest tile within 72 kB (x: 3 blocks of
-        // 256 per SM; y, z: 2 blocks of 256).  A mixed-form y or z tile
+        // Tile shape.  Default: the widest tile within 75 kB for x (3 blocks
+        // of 256 per SM), 72 kB for y and z (2 blocks of 256).  A mixed-form y or z tile
         // narrower than 16 lines there (z rows of 32 bytes or less per field)
         // instead takes one block of 512 threads per SM and the widest tile
         // within 200 kB: measured at 128^3, z 0.79 -> 0.70 ms per step; where
         // the 72 kB tile is already 16 lines wide (N = 42) one block per SM was
         // slower, its phases no longer overlapping another block's.
-        h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], d == 0 ? 1 : 0);
+        const int nb = sweep_nbuf(d, (int)h->tb);
+        h->L[d] = pick_L(h->tb, nb, Nd[d], d == 0 ? 1 : 0, d == 0 ? 75 : 72, true);
         h->threads[d] = h->mixed ? (d == 0 ? sweep_threads<float>(0) : 256) : sweep_threads<double>(d);
         if (h->mixed && d > 0 && h->L[d] < 16) {
-            h->L[d] = pick_L(h->tb, sweep_nbuf(d), Nd[d], 0, 200);
+            h->L[d] = pick_L(h->tb, nb, Nd[d], 0, 200, true);
             h->threads[d] = sweep_threads<float>(d);
         }
         h->Lf[d] = pick_L(h->tb, h->mixed ? 10 : 5, Nd[d], d == 0 ? 1 : 0);
@@ -643,22 +647,10 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
         // blocks per SM): HIT 256^3 filter 2.27 -> 1.81 ms per step; at
         // N = 128 the 8-line tile stays (16 lines measured slower)
         if (h->mixed && h->Lf[d] < 8) h->Lf[d] = pick_L(h->tb, 10, Nd[d], d == 0 ? 1 : 0, 110);
-        if (sweep_smem_bytes((int)h->tb, sweep_nbuf(d), 1, 2, Nd[d]) > 200 * 1024)
+        if (sweep_smem_bytes((int)h->tb, nb, 1, 2, Nd[d]) > 200 * 1024)
             return fail_free(fail(CS3D_ERR_SHAPE, "N[%d]=%d: a line does not fit in shared memory", d, Nd[d]));
     }
-    // The mixed form's z sweep runs pipelined where two slots of 8-line tiles
-    // fit in shared memory: one persistent 512-thread block per SM solves one
-    // tile while it consumes the previous one and loads the next.
-    if (h->mixed) {
-        const size_t slot = (sweep_smem_bytes(4, sweep_nbuf(2), 8, 8, Nd[2]) + 127) & ~(size_t)127;
-        int nsm = 0;
-        CS3D_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->dev));
-        const int ntiles = ((cfg->Nx + 7) / 8) * cfg->Ny;
-        if (2 * slot <= 220 * 1024 && nsm > 0) {
-            h->zslot_bytes = (int)slot;
-            h->zpipe_grid = ntiles < nsm ? ntiles : nsm;
-        }
-    }
+
     CS3D_CUDA(cudaStreamSynchronize(h->stream));
     *out = h;
     return CS3D_OK;
@@ -896,11 +888,8 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.sigma = h->sigma;
     a.savg = h->savg;
     for (int d = 0; d < 3; d++) {
-        const bool zpipe = d == 2 && sizeof(T) == 4 && h->zpipe_grid > 0 && h->zpipe_on;
-        a.pipe_grid = zpipe ? h->zpipe_grid : 0;
-        a.slot_bytes = h->zslot_bytes;
-        a.threads = zpipe ? z_pipe_threads() : h->threads[d];
-        a.L = zpipe ? 8 : h->L[d];
+        a.threads = h->threads[d];
+        a.L = h->L[d];
         a.lgL = ilog2(a.L);
         a.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
         a.P = a.L + (d == 0 ? 1 : 0);
@@ -1202,8 +1191,6 @@ extern "C" int cs3d_set_option(cs3d_handle *h, int option, int value) {
         h->store_diag = value != 0;
     } else if (option == CS3D_OPT_KERNEL_TIMING) {
         h->timing = value != 0;
-    } else if (option == CS3D_OPT_SWEEP_PIPELINE) {
-        h->zpipe_on = value != 0;
     } else {
         return fail(CS3D_ERR_ARG, "unknown option %d", option);
     }
@@ -1237,7 +1224,7 @@ static int line_op(cs3d_handle *h, int kind, int dir, const double *in, double *
     const int N = a.op.N;
     a.nlines = h->g.npts / N;
     a.L = 32;
-    while (a.L > 1 && sweep_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
+    while (a.L > 1 && planar_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
     a.P = a.L + 1;
     a.threads = 128;
     a.in = in;
@@ -1326,7 +1313,7 @@ static int op_launch(cs3d_op *o, int kind, const double *in, double *out) {
     const int N = a.op.N;
     a.nlines = o->npts / N;
     a.L = 32;
-    while (a.L > 1 && sweep_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
+    while (a.L > 1 && planar_smem_bytes(8, 1, a.L, a.L + 1, N) > 72 * 1024) a.L /= 2;
     a.P = a.L + 1;
     a.threads = 128;
     a.in = in;

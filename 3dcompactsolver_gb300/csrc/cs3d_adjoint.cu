@@ -246,7 +246,7 @@ template <typename T>
 cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s) {
     if (a.ntask < 1 || a.ntask > kApplyMax) return cudaErrorInvalidValue;
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
-    const size_t sm = sweep_smem_bytes((int)sizeof(T), a.ntask, a.L, a.P, N);
+    const size_t sm = planar_smem_bytes((int)sizeof(T), a.ntask, a.L, a.P, N);
     const int L = a.L;
     dim3 grid = dir == 0 ? dim3((a.g.Ny + L - 1) / L, a.g.Nz)
                          : dir == 1 ? dim3((a.g.Nx + L - 1) / L, a.g.Nz) : dim3((a.g.Nx + L - 1) / L, a.g.Ny);

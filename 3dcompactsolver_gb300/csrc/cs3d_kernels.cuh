@@ -77,10 +77,6 @@ struct SweepArgs {
     const double *sigma;
     Q5 savg;
     double *dq_out[5];  // increments dq (optional)
-    // pipelined z sweep (mixed form): persistent blocks and the bytes of one
-    // of their two shared-memory slots; pipe_grid 0 = one block per tile
-    int pipe_grid;
-    int slot_bytes;
 };
 
 template <typename T>
@@ -329,9 +325,11 @@ cudaError_t launch_lin5(const Lin5Args &a, cudaStream_t s);
 constexpr int kKeSeedBlocks = 512;
 cudaError_t launch_ke_seed(const KeSeedArgs &a, cudaStream_t s);
 
+// shared memory of a sweep tile (pair-interleaved for prec_bytes 4) and of
+// a planar tile (filter, single operators, adjoint operators)
 size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N);
-int z_pipe_threads();
-int sweep_nbuf(int dir);
+size_t planar_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N);
+int sweep_nbuf(int dir, int prec_bytes);
 int sweep_ntask(int dir);
 int filter_ntask();
 

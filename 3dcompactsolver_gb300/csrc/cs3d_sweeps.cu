@@ -73,17 +73,25 @@ namespace cs3d {
 // ---------------------------------------------------------------------
 // sweep x
 // ---------------------------------------------------------------------
-enum { XU = 0, XU2, XV, XV2, XW, XW2, XT, XT2, XRU, XF1, XF2, XF3, XF4, XNB };
+// Sweep task t solves into buffers 2t and 2t+1.  The FP32-mixed form's pair
+// layout gives the last task of the x and y sweeps (one field) a spare second
+// buffer (XDUM, YDUM) that its second, duplicate solve writes; the FP64 form
+// solves that field twice over in its own buffer.
+enum { XU = 0, XU2, XV, XV2, XW, XW2, XT, XT2, XRU, XF1, XF2, XF3, XF4, XDUM, XNB2 };
+constexpr int XNB = XDUM;
 __constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}, {XW, XW, 0, XW, XW2, 1},
                                 {XT, XT, 0, XT, XT2, 1}, {XRU, XRU, 0, XF1, XF1, 0},
                                 {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XF4, 0}};
+__constant__ Task kTasksX2[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}, {XW, XW, 0, XW, XW2, 1},
+                                 {XT, XT, 0, XT, XT2, 1}, {XRU, XRU, 0, XF1, XF1, 0},
+                                 {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XDUM, 0}};
 
 template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
-    Smem<T> sm = smem_layout<T>(XNB, L, P, N);
+    const auto sm = SweepSmem<T>::at(smem_raw, sizeof(T) == 4 ? XNB2 : XNB, L, P, N);
     const GasParams gp = a.gas;
     // phase A: primitives and the inputs of the x-solves
     struct InA { Pt pt; T q[5]; };
@@ -113,18 +121,17 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
                                    to_work<T>(a.backup.f[4][gi]));
             }
             const int o = in.pt.o;
-            sm.b(XU)[o] = ss.U;
-            sm.b(XV)[o] = ss.V;
-            sm.b(XW)[o] = ss.W;
-            sm.b(XT)[o] = ss.Tt;
-            sm.b(XRU)[o] = s.ru;
-            sm.b(XF1)[o] = s.ru * ss.U + ss.p;
-            sm.b(XF2)[o] = s.rv * ss.U;
-            sm.b(XF3)[o] = s.rw * ss.U;
-            sm.b(XF4)[o] = s.re * ss.U + ss.U * ss.p;
+            put1(sm, 0, o, ss.U);
+            put1(sm, 1, o, ss.V);
+            put1(sm, 2, o, ss.W);
+            put1(sm, 3, o, ss.Tt);
+            put2(sm, 4, o, s.ru, s.ru * ss.U + ss.p);
+            put2(sm, 5, o, s.rv * ss.U, s.rw * ss.U);
+            put1(sm, 6, o, s.re * ss.U + ss.U * ss.p);
         });
     __syncthreads();
-    run_tasks<T, 2, PC>(sm, kTasksX, 7, L, t.nlines, a.d1, a.d2);
+    run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksX2 : kTasksX, 7, L, t.nlines, a.d1, a.d2, threadIdx.x,
+                           blockDim.x);
     __syncthreads();
     // phase C
     const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
@@ -145,13 +152,14 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
             const T amu = (T)0.76 * mu / Tt;
             a.mu[gi] = mu;
             a.amu[gi] = amu;
-            const T Ux = gz(sm, XU, p, L, zz.z1), Uxx = gz(sm, XU2, p, L, zz.z2);
-            const T Vx = gz(sm, XV, p, L, zz.z1), Vxx = gz(sm, XV2, p, L, zz.z2);
-            const T Wx = gz(sm, XW, p, L, zz.z1), Wxx = gz(sm, XW2, p, L, zz.z2);
-            const T Tx = gz(sm, XT, p, L, zz.z1), Txx = gz(sm, XT2, p, L, zz.z2);
-            const T cex = gz(sm, XRU, p, L, zz.z1);
-            const T f1 = gz(sm, XF1, p, L, zz.z1), f2 = gz(sm, XF2, p, L, zz.z1);
-            const T f3 = gz(sm, XF3, p, L, zz.z1), f4 = gz(sm, XF4, p, L, zz.z1);
+            T Ux, Uxx, Vx, Vxx, Wx, Wxx, Tx, Txx, cex, f1, f2, f3;
+            get2(sm, 0, p, L, zz.z1, zz.z2, Ux, Uxx);
+            get2(sm, 1, p, L, zz.z1, zz.z2, Vx, Vxx);
+            get2(sm, 2, p, L, zz.z1, zz.z2, Wx, Wxx);
+            get2(sm, 3, p, L, zz.z1, zz.z2, Tx, Txx);
+            get2(sm, 4, p, L, zz.z1, zz.z1, cex, f1);
+            get2(sm, 5, p, L, zz.z1, zz.z1, f2, f3);
+            const T f4 = get1(sm, XF4, p, L, zz.z1);
             a.dx[0][gi] = Ux; a.dx[1][gi] = Vx; a.dx[2][gi] = Wx; a.dx[3][gi] = Tx;
             a.R[0][gi] = -cex;
             a.R[1][gi] = mu * (c43 * Uxx) - f1;
@@ -164,18 +172,23 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
 // ---------------------------------------------------------------------
 // sweep y
 // ---------------------------------------------------------------------
-enum { YU = 0, YU2, YV, YV2, YW, YW2, YT, YT2, YUX, YVX, YRV, YF1, YF2, YF3, YF4, YNB };
+enum { YU = 0, YU2, YV, YV2, YW, YW2, YT, YT2, YUX, YVX, YRV, YF1, YF2, YF3, YF4, YDUM, YNB2 };
+constexpr int YNB = YDUM;
 __constant__ Task kTasksY[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}, {YW, YW, 0, YW, YW2, 1},
                                 {YT, YT, 0, YT, YT2, 1}, {YUX, YUX, 0, YVX, YVX, 0},
                                 {YRV, YRV, 0, YF1, YF1, 0}, {YF2, YF2, 0, YF3, YF3, 0},
                                 {YF4, YF4, 0, YF4, YF4, 0}};
+__constant__ Task kTasksY2[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1}, {YW, YW, 0, YW, YW2, 1},
+                                 {YT, YT, 0, YT, YT2, 1}, {YUX, YUX, 0, YVX, YVX, 0},
+                                 {YRV, YRV, 0, YF1, YF1, 0}, {YF2, YF2, 0, YF3, YF3, 0},
+                                 {YF4, YF4, 0, YF4, YDUM, 0}};
 
 template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
-    Smem<T> sm = smem_layout<T>(YNB, L, P, N);
+    const auto sm = SweepSmem<T>::at(smem_raw, sizeof(T) == 4 ? YNB2 : YNB, L, P, N);
     struct InA { Pt pt; T v[11]; };
     batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
         [&](InA &in, int p) {
@@ -193,20 +206,18 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
             const int o = in.pt.o;
             const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
             const T V = in.v[5], pp = in.v[7];
-            sm.b(YU)[o] = in.v[4];
-            sm.b(YV)[o] = V;
-            sm.b(YW)[o] = in.v[6];
-            sm.b(YT)[o] = in.v[8];
-            sm.b(YUX)[o] = in.v[9];
-            sm.b(YVX)[o] = in.v[10];
-            sm.b(YRV)[o] = rv;
-            sm.b(YF1)[o] = ru * V;
-            sm.b(YF2)[o] = rv * V + pp;
-            sm.b(YF3)[o] = rw * V;
-            sm.b(YF4)[o] = re * V + V * pp;
+            put1(sm, 0, o, in.v[4]);
+            put1(sm, 1, o, V);
+            put1(sm, 2, o, in.v[6]);
+            put1(sm, 3, o, in.v[8]);
+            put2(sm, 4, o, in.v[9], in.v[10]);
+            put2(sm, 5, o, rv, ru * V);
+            put2(sm, 6, o, rv * V + pp, rw * V);
+            put1(sm, 7, o, re * V + V * pp);
         });
     __syncthreads();
-    run_tasks<T, 2, PC>(sm, kTasksY, 8, L, t.nlines, a.d1, a.d2);
+    run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksY2 : kTasksY, 8, L, t.nlines, a.d1, a.d2, threadIdx.x,
+                           blockDim.x);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
@@ -225,14 +236,15 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
             const unsigned gi = p.gi;
             const Zn<T> zz = zn(a.d1, a.d2, p.n);
             const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3];
-            const T Uy = gz(sm, YU, p, L, zz.z1), Uyy = gz(sm, YU2, p, L, zz.z2);
-            const T Vy = gz(sm, YV, p, L, zz.z1), Vyy = gz(sm, YV2, p, L, zz.z2);
-            const T Wy = gz(sm, YW, p, L, zz.z1), Wyy = gz(sm, YW2, p, L, zz.z2);
-            const T Ty = gz(sm, YT, p, L, zz.z1), Tyy = gz(sm, YT2, p, L, zz.z2);
-            const T Uxy = gz(sm, YUX, p, L, zz.z1), Vxy = gz(sm, YVX, p, L, zz.z1);
-            const T cey = gz(sm, YRV, p, L, zz.z1);
-            const T f1 = gz(sm, YF1, p, L, zz.z1), f2 = gz(sm, YF2, p, L, zz.z1);
-            const T f3 = gz(sm, YF3, p, L, zz.z1), f4 = gz(sm, YF4, p, L, zz.z1);
+            T Uy, Uyy, Vy, Vyy, Wy, Wyy, Ty, Tyy, Uxy, Vxy, cey, f1, f2, f3;
+            get2(sm, 0, p, L, zz.z1, zz.z2, Uy, Uyy);
+            get2(sm, 1, p, L, zz.z1, zz.z2, Vy, Vyy);
+            get2(sm, 2, p, L, zz.z1, zz.z2, Wy, Wyy);
+            get2(sm, 3, p, L, zz.z1, zz.z2, Ty, Tyy);
+            get2(sm, 4, p, L, zz.z1, zz.z1, Uxy, Vxy);
+            get2(sm, 5, p, L, zz.z1, zz.z1, cey, f1);
+            get2(sm, 6, p, L, zz.z1, zz.z1, f2, f3);
+            const T f4 = get1(sm, YF4, p, L, zz.z1);
             a.dy[0][gi] = Uy; a.dy[1][gi] = Vy; a.dy[2][gi] = Wy; a.dy[3][gi] = Ty;
             int i, j, k;
             coords<1>(t, p.l, p.n, i, j, k);
@@ -256,15 +268,13 @@ __constant__ Task kTasksZ[8] = {{ZU, ZU, 0, ZU, ZU2, 1}, {ZV, ZV, 0, ZV, ZV2, 1}
                                 {ZWY, ZWY, 0, ZRW, ZRW, 0}, {ZF1, ZF1, 0, ZF2, ZF2, 0},
                                 {ZF3, ZF3, 0, ZF4, ZF4, 0}};
 
-// The z sweep's three phases as functions of (tile, shared-memory slot,
-// thread range), so that the one-tile kernel (all threads run A, B, C in
-// turn) and the pipelined kernel (solver warps run B of one tile while the
-// other warps run C of the previous tile and A of the next) execute the same
-// per-point arithmetic in the same order: their results are identical.
+// The z sweep's three phases as functions of (tile, shared-memory layout,
+// thread range).
 template <typename T, int PC>
 struct ZSweep {
     // A: stage the inputs of the 16 z-solves of tile t in sm
-    static __device__ __forceinline__ void load(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+    using SM = typename SweepSmem<T>::type;
+    static __device__ __forceinline__ void load(const SweepArgs<T> &a, const Tile &t, const SM &sm, int tid,
                                                 int nthr) {
         const int L = a.L, P = PC > 0 ? PC : a.P;
         const int NL = t.N * L;
@@ -287,27 +297,23 @@ struct ZSweep {
                 const int o = in.pt.o;
                 const T ru = in.v[0], rv = in.v[1], rw = in.v[2], re = in.v[3];
                 const T W = in.v[6], pp = in.v[7];
-                sm.b(ZU)[o] = in.v[4];
-                sm.b(ZV)[o] = in.v[5];
-                sm.b(ZW)[o] = W;
-                sm.b(ZT)[o] = in.v[8];
-                sm.b(ZS)[o] = in.v[9] + in.v[10];
-                sm.b(ZWX)[o] = in.v[11];
-                sm.b(ZWY)[o] = in.v[12];
-                sm.b(ZRW)[o] = rw;
-                sm.b(ZF1)[o] = ru * W;
-                sm.b(ZF2)[o] = rv * W;
-                sm.b(ZF3)[o] = rw * W + pp;
-                sm.b(ZF4)[o] = re * W + W * pp;
+                put1(sm, 0, o, in.v[4]);
+                put1(sm, 1, o, in.v[5]);
+                put1(sm, 2, o, W);
+                put1(sm, 3, o, in.v[8]);
+                put2(sm, 4, o, in.v[9] + in.v[10], in.v[11]);
+                put2(sm, 5, o, in.v[12], rw);
+                put2(sm, 6, o, ru * W, rv * W);
+                put2(sm, 7, o, rw * W + pp, re * W + W * pp);
             });
     }
     // B: the 16 solves (8 pairs) of every line of the tile
-    static __device__ __forceinline__ void solve(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+    static __device__ __forceinline__ void solve(const SweepArgs<T> &a, const Tile &t, const SM &sm, int tid,
                                                  int nthr) {
-        run_tasks<T, 2, PC>(sm, kTasksZ, 8, a.L, t.nlines, a.d1, a.d2, tid, nthr);
+        run_sweep_tasks<2, PC>(sm, kTasksZ, 8, a.L, t.nlines, a.d1, a.d2, tid, nthr);
     }
     // C: right-hand side, dq and the RK update of every point of the tile
-    static __device__ __forceinline__ void consume(const SweepArgs<T> &a, const Tile &t, const Smem<T> &sm, int tid,
+    static __device__ __forceinline__ void consume(const SweepArgs<T> &a, const Tile &t, const SM &sm, int tid,
                                                    int nthr) {
         const int L = a.L, P = PC > 0 ? PC : a.P;
         const int NL = t.N * L;
@@ -360,15 +366,15 @@ struct ZSweep {
                 const T U = in.v[0], V = in.v[1], W = in.v[2], mu = in.v[3], amu = in.v[4];
                 const T Ux = in.v[5], Vx = in.v[6], Wx = in.v[7], Tx = in.v[8];
                 const T Uy = in.v[9], Vy = in.v[10], Wy = in.v[11], Ty = in.v[12];
-                const T Uz = gz(sm, ZU, p, L, zz.z1), Uzz = gz(sm, ZU2, p, L, zz.z2);
-                const T Vz = gz(sm, ZV, p, L, zz.z1), Vzz = gz(sm, ZV2, p, L, zz.z2);
-                const T Wz = gz(sm, ZW, p, L, zz.z1), Wzz = gz(sm, ZW2, p, L, zz.z2);
-                const T Tz = gz(sm, ZT, p, L, zz.z1), Tzz = gz(sm, ZT2, p, L, zz.z2);
-                const T S = gz(sm, ZS, p, L, zz.z1);  // Uxz + Vyz
-                const T Wxz = gz(sm, ZWX, p, L, zz.z1), Wyz = gz(sm, ZWY, p, L, zz.z1);
-                const T cez = gz(sm, ZRW, p, L, zz.z1);
-                const T f1 = gz(sm, ZF1, p, L, zz.z1), f2 = gz(sm, ZF2, p, L, zz.z1);
-                const T f3 = gz(sm, ZF3, p, L, zz.z1), f4 = gz(sm, ZF4, p, L, zz.z1);
+                T Uz, Uzz, Vz, Vzz, Wz, Wzz, Tz, Tzz, S, Wxz, Wyz, cez, f1, f2, f3, f4;
+                get2(sm, 0, p, L, zz.z1, zz.z2, Uz, Uzz);
+                get2(sm, 1, p, L, zz.z1, zz.z2, Vz, Vzz);
+                get2(sm, 2, p, L, zz.z1, zz.z2, Wz, Wzz);
+                get2(sm, 3, p, L, zz.z1, zz.z2, Tz, Tzz);
+                get2(sm, 4, p, L, zz.z1, zz.z1, S, Wxz);  // S = d/dz (Ux + Vy)
+                get2(sm, 5, p, L, zz.z1, zz.z1, Wyz, cez);
+                get2(sm, 6, p, L, zz.z1, zz.z1, f1, f2);
+                get2(sm, 7, p, L, zz.z1, zz.z1, f3, f4);
                 T src[5] = {T(0), T(0), T(0), T(0), T(0)};
                 if (a.sponge) {  // sigma (avg - q), SpongeBC / CSolver_AWS.hpp:228
                     const T sg = to_work<T>(a.sigma[gi]);
@@ -413,7 +419,7 @@ struct ZSweep {
                     T d = sizeof(T) == 8 ? (T)(dt * (double)R[f]) : dtw * R[f];
                     if (zero_all || (f > 0 && zero_mom)) d = T(0);
                     if (a.dq_out[0]) a.dq_out[f][gi] = to_f64(d);
-                    sm.b(kDq[f])[p.o] = d;
+                    sm.at(kDq[f], p.o) = d;
                 }
             });
         struct InC2 {
@@ -439,7 +445,7 @@ struct ZSweep {
                     // plain form: the reference's RK update in FP64
 #pragma unroll
                     for (int f = 0; f < 5; ++f) {
-                        const double d = (double)sm.b(kDq[f])[in.pt.o];
+                        const double d = (double)sm.at(kDq[f], in.pt.o);
                         if (tvd) {  // TVD-RK3 (TVDRK3.hpp:38-96); qa = q1, qb = qk
                             if (st == 1) a.qk.f[f][gi] = in.qa[f] + d;
                             else if (st == 2) a.qk.f[f][gi] = 0.75 * in.qa[f] + 0.25 * in.qb[f] + 0.25 * d;
@@ -456,7 +462,7 @@ struct ZSweep {
                     // mixed form: the FP32 increment accumulated into the FP64 state
 #pragma unroll
                     for (int f = 0; f < 5; ++f) {
-                        const T d = sm.b(kDq[f])[in.pt.o];
+                        const T d = sm.at(kDq[f], in.pt.o);
                         if (tvd) {
                             const double dd = to_f64(d);
                             double nv;
@@ -488,54 +494,12 @@ struct ZSweep {
 template <typename T, int PC>
 __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
     const Tile t = make_tile<2>(a.g, a.L);
-    const Smem<T> sm = smem_layout<T>(ZNB, a.L, PC > 0 ? PC : a.P, t.N);
+    const auto sm = SweepSmem<T>::at(smem_raw, ZNB, a.L, PC > 0 ? PC : a.P, t.N);
     ZSweep<T, PC>::load(a, t, sm, threadIdx.x, blockDim.x);
     __syncthreads();
     ZSweep<T, PC>::solve(a, t, sm, threadIdx.x, blockDim.x);
     __syncthreads();
     ZSweep<T, PC>::consume(a, t, sm, threadIdx.x, blockDim.x);
-}
-
-// The pipelined z sweep (FP32-mixed form): one persistent block per SM walks
-// the tiles b, b + G, b + 2G, ... (G = gridDim.x) with two shared-memory
-// slots.  In iteration k the first kZSolveWarps warps solve tile k (slot
-// k & 1) while the other warps consume tile k - 1 and then load tile k + 1
-// into the slot tile k - 1 leaves (a barrier among those warps separates the
-// two), so the solve phase, which touches no global memory, runs while the
-// other warps stream.  One block barrier per iteration hands the slots over.
-constexpr int kZSolveWarps = 2;
-constexpr int kZPipeThreads = 512;
-
-template <int PC>
-__global__ void __launch_bounds__(kZPipeThreads, 1) k_sweep_z_pipe(SweepArgs<float> a) {
-    using Z = ZSweep<float, PC>;
-    const int L = a.L, P = PC > 0 ? PC : a.P;
-    const int nxb = (a.g.Nx + L - 1) / L, ntiles = nxb * a.g.Ny;
-    const int G = gridDim.x, b = blockIdx.x;
-    const Smem<float> s0 = smem_layout<float>(ZNB, L, P, a.g.Nz);
-    const Smem<float> s1 = smem_layout_at<float>(smem_raw + a.slot_bytes, ZNB, L, P, a.g.Nz);
-    const int nsolve = 32 * kZSolveWarps;
-    const bool solver = (int)threadIdx.x < nsolve;
-    const int mtid = (int)threadIdx.x - nsolve, mthr = (int)blockDim.x - nsolve;
-    auto tile = [&](int tt) { return make_tile_at<2>(a.g, L, tt % nxb, tt / nxb); };
-    if (!solver && b < ntiles) Z::load(a, tile(b), s0, mtid, mthr);
-    __syncthreads();
-    for (int k = 0;; ++k) {
-        const int tk = b + k * G;  // solved in this iteration
-        if (tk - G >= ntiles) break;
-        const Smem<float> &cur = (k & 1) ? s1 : s0;
-        const Smem<float> &oth = (k & 1) ? s0 : s1;
-        if (solver) {
-            if (tk < ntiles) Z::solve(a, tile(tk), cur, threadIdx.x, nsolve);
-        } else {
-            if (k > 0) Z::consume(a, tile(tk - G), oth, mtid, mthr);
-            if (tk + G < ntiles) {
-                asm volatile("bar.sync 1, %0;" ::"r"(mthr) : "memory");
-                Z::load(a, tile(tk + G), oth, mtid, mthr);
-            }
-        }
-        __syncthreads();
-    }
 }
 
 // ---------------------------------------------------------------------
@@ -671,12 +635,23 @@ static size_t tile_smem(int nbuf, int L, int P, int N) {
     return sizeof(T) * ((size_t)nf + (size_t)nbuf * buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4)));
 }
 
-int z_pipe_threads() { return kZPipeThreads; }
+// The FP32-mixed sweeps' pair-interleaved tiles: the per-line factors, then
+// (nbuf + 1) / 2 pair arrays.
+static size_t pair_tile_smem(int nbuf, int L, int P, int N) {
+    const int nf = (nbuf * L + 3) & ~3;
+    return 4 * ((size_t)nf + (size_t)((nbuf + 1) / 2) * pair_stride(N + kPad, P));
+}
 
-size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
+size_t planar_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
     return prec_bytes == 8 ? tile_smem<double>(nbuf, L, P, N) : tile_smem<float>(nbuf, L, P, N);
 }
-int sweep_nbuf(int dir) { return dir == 0 ? (int)XNB : dir == 1 ? (int)YNB : (int)ZNB; }
+size_t sweep_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {
+    return prec_bytes == 8 ? tile_smem<double>(nbuf, L, P, N) : pair_tile_smem(nbuf, L, P, N);
+}
+int sweep_nbuf(int dir, int prec_bytes) {
+    if (prec_bytes == 4) return dir == 0 ? (int)XNB2 : dir == 1 ? (int)YNB2 : (int)ZNB;
+    return dir == 0 ? (int)XNB : dir == 1 ? (int)YNB : (int)ZNB;
+}
 int sweep_ntask(int dir) { return dir == 0 ? 7 : 8; }
 int filter_ntask() { return 3; }
 
@@ -697,16 +672,9 @@ static dim3 tile_grid(int dir, const Geom &g, int L) {
 template <typename T>
 cudaError_t launch_sweep(int dir, const SweepArgs<T> &a, cudaStream_t s) {
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
-    const size_t sm = tile_smem<T>(sweep_nbuf(dir), a.L, a.P, N);
+    const size_t sm = sweep_smem_bytes((int)sizeof(T), sweep_nbuf(dir, (int)sizeof(T)), a.L, a.P, N);
     const dim3 grid = tile_grid(dir, a.g, a.L);
     if constexpr (sizeof(T) == 4) {
-        if (dir == 2 && a.pipe_grid > 0 && a.P == 8) {
-            cudaError_t e = cudaFuncSetAttribute(k_sweep_z_pipe<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 2 * a.slot_bytes);
-            if (e != cudaSuccess) return e;
-            k_sweep_z_pipe<8><<<a.pipe_grid, kZPipeThreads, 2 * a.slot_bytes, s>>>(a);
-            return cudaGetLastError();
-        }
         if (dir == 0 && a.P == 9) return launch_tile_kernel(k_sweep_x<T, 9>, a, grid, sm, s);
         if (dir == 0 && a.P == 5) return launch_tile_kernel(k_sweep_x<T, 5>, a, grid, sm, s);
         if (dir == 1 && a.P == 16) return launch_tile_kernel(k_sweep_y<T, 16>, a, grid, sm, s);

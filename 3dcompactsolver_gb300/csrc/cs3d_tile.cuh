@@ -258,6 +258,176 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
     *fb = ob.periodic ? (T)((to_f64(xb) + ob.bog * to_f64(xlb)) * ob.inv_den) : T(0);
 }
 
+// ---------------------------------------------------------------------
+// paired FP32 line solves on pair-interleaved lines (the FP32-mixed sweeps)
+// ---------------------------------------------------------------------
+// The two solves of a task keep their lines pair-interleaved in shared
+// memory: element n of the pair is the float2 pr[n*P], lane x holding solve
+// A's line and lane y solve B's, so a row of both is one 64-bit load or
+// store.  Each solve reads its own lane and writes it in place (where both
+// solves differentiate one field, the load phase stores the field in both
+// lanes).  The arithmetic is per lane, the operations and their order those
+// of solve_pair, so the results are the same bit for bit.  (The packed f32x2
+// multiply-add was measured too: no faster than two scalar ones here.)
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+
+template <int H, int PC>
+__device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa, float *fa, const LineOp<float> &ob,
+                                            float *fb, int P_) {
+    constexpr int W = 2 * H + 1;
+    const int P = PC > 0 ? PC : P_;
+    const int N = oa.N;
+    const float *lx = reinterpret_cast<const float *>(pr);
+    float pa[2 * H], pb[2 * H];
+    boundary_rows<float, H>(lx, 2 * P, oa, pa);
+    boundary_rows<float, H>(lx + 1, 2 * P, ob, pb);
+    float2 t2[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) t2[k] = make_float2(oa.taps[kMaxH - H + k], ob.taps[kMaxH - H + k]);
+    const float *__restrict__ ma = oa.m;
+    const float *__restrict__ mb = ob.m;
+    // window of the first interior row H: positions 0..2H
+    float2 w[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) w[k] = pr[k * P];
+    // rows 0..H-1
+    float2 y = make_float2(pa[0], pb[0]);
+    pr[0] = y;
+#pragma unroll
+    for (int n = 1; n < H; ++n) {
+        y = ffma2(make_float2(-ldc(&ma[n]), -ldc(&mb[n])), y, make_float2(pa[n], pb[n]));
+        pr[n * P] = y;
+    }
+    // interior rows H..N-H-1 in chunks of kU (as solve_pair: chunks inside
+    // [klo, khi) of both operators on the register constants)
+    const int nend = N - H;
+    int n = H;
+    const int klo = max(oa.klo, ob.klo), khi = min(oa.khi, ob.khi);
+    const int clo = H + kU * ((max(klo - H, 0) + kU - 1) / kU);
+    const float2 km2 = make_float2(-oa.km, -ob.km);
+    float2 nx[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) nx[j] = pr[(n + H + 1 + j) * P];
+    float ma4[kU], mb4[kU];
+    load4(oa.mf, ma4);
+    load4(ob.mf, mb4);
+    auto fwd_chunk = [&](auto kconst) {
+        constexpr bool K = decltype(kconst)::value;
+        float2 c[kU], mc[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            c[j] = nx[j];
+            mc[j] = K ? km2 : make_float2(-ma4[j], -mb4[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) nx[j] = pr[(n + kU + H + 1 + j) * P];
+        if (!K) {
+            load4(oa.mf + (n + kU - H), ma4);
+            load4(ob.mf + (n + kU - H), mb4);
+        }
+        float2 e[W + kU];
+#pragma unroll
+        for (int k = 0; k < W; ++k) e[k] = w[k];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) e[W + j] = c[j];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < W; ++k) acc = ffma2(t2[k], e[j + k], acc);
+            y = ffma2(mc[j], y, acc);
+            pr[(n + j) * P] = y;
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) w[k] = e[kU + k];
+    };
+    for (; n + kU <= nend && n < clo; n += kU) fwd_chunk(std::false_type{});
+    if (n + kU <= khi) {
+#pragma unroll 2
+        for (; n + kU <= nend && n + kU <= khi; n += kU) fwd_chunk(std::true_type{});
+        load4(oa.mf + (n - H), ma4);
+        load4(ob.mf + (n - H), mb4);
+    }
+#pragma unroll 2
+    for (; n + kU <= nend; n += kU) fwd_chunk(std::false_type{});
+    for (; n < nend; ++n) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < W; ++k) acc = ffma2(t2[k], w[k], acc);
+        y = ffma2(make_float2(-ldc(&ma[n]), -ldc(&mb[n])), y, acc);
+#pragma unroll
+        for (int k = 0; k < W - 1; ++k) w[k] = w[k + 1];
+        const int pos = n + H + 1;
+        w[W - 1] = pos < N ? pr[pos * P] : make_float2(0.f, 0.f);
+        pr[n * P] = y;
+    }
+    // rows N-H..N-1
+#pragma unroll
+    for (int b = 0; b < H; ++b) {
+        const int r = N - H + b;
+        y = ffma2(make_float2(-ldc(&ma[r]), -ldc(&mb[r])), y, make_float2(pa[H + b], pb[H + b]));
+        pr[r * P] = y;
+    }
+    // back substitution in chunks of kU, next chunk prefetched
+    const float *__restrict__ ca_ = oa.c;
+    const float *__restrict__ cb_ = ob.c;
+    const float *__restrict__ ia = oa.iw;
+    const float *__restrict__ ib = ob.iw;
+    float2 x = fmul2(y, make_float2(ldc(&ia[N - 1]), ldc(&ib[N - 1])));
+    pr[(N - 1) * P] = x;
+    const float2 xl = x;
+    n = N - 2;
+    float2 y4[kU];
+#pragma unroll
+    for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - j, 0) * P];
+    float cA[kU], cB[kU], iA[kU], iB[kU];
+    load4(oa.cbk, cA); load4(ob.cbk, cB);
+    load4(oa.ibk, iA); load4(ob.ibk, iB);
+    const float2 kc2 = make_float2(-oa.kc, -ob.kc), ki2 = make_float2(oa.kiw, ob.kiw);
+    auto bwd_chunk = [&](auto kconst) {
+        constexpr bool K = decltype(kconst)::value;
+        float2 y0[kU], c0[kU], i0[kU];
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            y0[j] = y4[j];
+            c0[j] = K ? kc2 : make_float2(-cA[j], -cB[j]);
+            i0[j] = K ? ki2 : make_float2(iA[j], iB[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - kU - j, 0) * P];
+        if (!K) {
+            const int kb = N - 2 - (n - kU);
+            load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+            load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+        }
+#pragma unroll
+        for (int j = 0; j < kU; ++j) {
+            x = fmul2(ffma2(c0[j], x, y0[j]), i0[j]);
+            pr[(n - j) * P] = x;
+        }
+    };
+    for (; n - kU + 1 >= 0 && n >= khi; n -= kU) bwd_chunk(std::false_type{});
+    if (n - kU + 1 >= klo) {
+#pragma unroll 2
+        for (; n - kU + 1 >= klo; n -= kU) bwd_chunk(std::true_type{});
+        const int kb = N - 2 - n;
+        load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
+        load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
+    }
+#pragma unroll 2
+    for (; n - kU + 1 >= 0; n -= kU) bwd_chunk(std::false_type{});
+    for (; n >= 0; --n) {
+        x = fmul2(ffma2(make_float2(-ldc(&ca_[n]), -ldc(&cb_[n])), x, pr[n * P]),
+                  make_float2(ldc(&ia[n]), ldc(&ib[n])));
+        pr[n * P] = x;
+    }
+    *fa = oa.periodic ? (float)((to_f64(x.x) + oa.bog * to_f64(xl.x)) * oa.inv_den) : 0.f;
+    *fb = ob.periodic ? (float)((to_f64(x.y) + ob.bog * to_f64(xl.y)) * ob.inv_den) : 0.f;
+}
+
 // Row n of the explicit right-hand side of a line read from src (stride P):
 // the interior stencil, or the explicit boundary row (wrapped columns), with
 // the products summed in the same order as solve_pair.
@@ -465,7 +635,28 @@ struct Smem {
     int bstride;
     int P;
     __device__ T *b(int k) const { return buf + (size_t)k * bstride; }
+    __device__ T &at(int k, int o) const { return buf[(size_t)k * bstride + o]; }
 };
+
+// Pair-interleaved layout of the FP32-mixed sweep tiles: buffers 2t and
+// 2t+1 (the two solves of task t) share one float2 array, element (n, l) of
+// the pair at float2 index n*P + l; pairs pstride floats apart, pstride = 16
+// (mod 32) so that the two tasks of a half-warp's 64-bit accesses cover
+// distinct banks.  Per-line factors stay planar: fact[k*L + l].
+struct SmemPair {
+    float *buf;
+    float *fact;
+    int pstride;
+    int P;
+    __device__ float2 *pair(int t) const { return reinterpret_cast<float2 *>(buf + (size_t)t * pstride); }
+    __device__ float &at(int k, int o) const { return buf[(size_t)(k >> 1) * pstride + 2 * o + (k & 1)]; }
+};
+
+__host__ __device__ inline int pair_stride(int N, int P) {
+    int st = 2 * N * P;
+    st += ((16 - st % 32) + 32) % 32;
+    return st;
+}
 
 // Elements between consecutive buffers.  The solve tasks of one warp use
 // buffers two apart (A solves 0,2,4,..; B solves 1,3,5,..), each touching L
@@ -491,6 +682,33 @@ __device__ __forceinline__ Smem<T> smem_layout_at(unsigned char *base, int nbuf,
 }
 
 extern __shared__ __align__(16) unsigned char smem_raw[];
+
+__device__ __forceinline__ SmemPair smem_pair_at(unsigned char *base, int nbuf, int L, int P, int N) {
+    SmemPair s;
+    s.P = P;
+    s.pstride = pair_stride(N + kPad, P);
+    s.fact = reinterpret_cast<float *>(base);
+    const int nf = (nbuf * L + 3) & ~3;
+    s.buf = reinterpret_cast<float *>(base) + nf;
+    return s;
+}
+
+// The sweep kernels' tile layout: pair-interleaved in the FP32-mixed form,
+// planar in the FP64 form.
+template <typename T>
+struct SweepSmem {
+    using type = Smem<T>;
+    static __device__ __forceinline__ type at(unsigned char *base, int nbuf, int L, int P, int N) {
+        return smem_layout_at<T>(base, nbuf, L, P, N);
+    }
+};
+template <>
+struct SweepSmem<float> {
+    using type = SmemPair;
+    static __device__ __forceinline__ type at(unsigned char *base, int nbuf, int L, int P, int N) {
+        return smem_pair_at(base, nbuf, L, P, N);
+    }
+};
 
 template <typename T>
 __device__ __forceinline__ Smem<T> smem_layout(int nbuf, int L, int P, int N) {
@@ -600,6 +818,64 @@ template <typename T, int H, int PC = 0>
 __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
                                           const LineOp<T> &op0, const LineOp<T> &op1) {
     run_tasks<T, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, (int)threadIdx.x, (int)blockDim.x);
+}
+
+// The tasks of a sweep tile; sweep task t solves into buffers 2t and 2t+1.
+// FP32-mixed: paired solves on the pair-interleaved layout; FP64: solve_pair
+// on the planar layout.
+template <int H, int PC>
+__device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *tasks, int ntask, int L, int nlines,
+                                                const LineOp<float> &op0, const LineOp<float> &op1, int tid,
+                                                int nthr) {
+    for (int w = tid; w < ntask * L; w += nthr) {
+        const int t = w / L, l = w - t * L;
+        if (l >= nlines) continue;
+        const Task tk = tasks[t];
+        const LineOp<float> &oa = tk.oa == 1 ? op1 : op0;
+        const LineOp<float> &ob = tk.ob == 1 ? op1 : op0;
+        solve_pair2<H, PC>(sm.pair(tk.da >> 1) + l, oa, &sm.fact[tk.da * L + l], ob, &sm.fact[tk.db * L + l], sm.P);
+    }
+}
+template <int H, int PC>
+__device__ __forceinline__ void run_sweep_tasks(const Smem<double> &sm, const Task *tasks, int ntask, int L,
+                                                int nlines, const LineOp<double> &op0, const LineOp<double> &op1,
+                                                int tid, int nthr) {
+    run_tasks<double, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, tid, nthr);
+}
+
+// Phase-A stores of task t's inputs at offset o: put1 for a task whose two
+// solves read one field, put2 for two fields.  In the pair layout both are
+// one 64-bit store (put1 stores the field in both lanes); in the planar
+// layout put1 stores the field once, in the first buffer.
+__device__ __forceinline__ void put1(const SmemPair &sm, int t, int o, float v) { sm.pair(t)[o] = make_float2(v, v); }
+__device__ __forceinline__ void put2(const SmemPair &sm, int t, int o, float v0, float v1) {
+    sm.pair(t)[o] = make_float2(v0, v1);
+}
+template <typename T>
+__device__ __forceinline__ void put1(const Smem<T> &sm, int t, int o, T v) { sm.at(2 * t, o) = v; }
+template <typename T>
+__device__ __forceinline__ void put2(const Smem<T> &sm, int t, int o, T v0, T v1) {
+    sm.at(2 * t, o) = v0;
+    sm.at(2 * t + 1, o) = v1;
+}
+
+// Corrected solutions (Sherman-Morrison term -f z, f the buffer's line factor,
+// z the operator's vector at the point) of task t's two buffers at point p,
+// and of one buffer k.
+__device__ __forceinline__ void get2(const SmemPair &sm, int t, const Pt &p, int L, float za, float zb, float &a,
+                                     float &b) {
+    const float2 v = sm.pair(t)[p.o];
+    a = fmaf(-sm.fact[(2 * t) * L + p.l], za, v.x);
+    b = fmaf(-sm.fact[(2 * t + 1) * L + p.l], zb, v.y);
+}
+template <typename T>
+__device__ __forceinline__ void get2(const Smem<T> &sm, int t, const Pt &p, int L, T za, T zb, T &a, T &b) {
+    a = fma(-sm.fact[(2 * t) * L + p.l], za, sm.at(2 * t, p.o));
+    b = fma(-sm.fact[(2 * t + 1) * L + p.l], zb, sm.at(2 * t + 1, p.o));
+}
+template <typename SM, typename T>
+__device__ __forceinline__ T get1(const SM &sm, int k, const Pt &p, int L, T z) {
+    return fma(-sm.fact[k * L + p.l], z, sm.at(k, p.o));
 }
 
 template <typename T>

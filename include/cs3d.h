@@ -165,7 +165,7 @@ int cs3d_get_stream(cs3d_handle *h, void **stream);
 /* Number of kernels the handle has launched so far. */
 int cs3d_launch_count(cs3d_handle *h, long long *count);
 
-/* Options (value 0 = off, the default, except where stated):
+/* Options (value 0 = off, the default):
  *  CS3D_OPT_STORE_INCREMENTS  keep the stage increments dt*RHS (rhok2..rhoEk2,
  *                             CSolver_AWS.cpp:1246-1504) in device memory;
  *  CS3D_OPT_STORE_DIAGNOSTICS keep Uz, Vz, Wz of the last stage so that
@@ -173,12 +173,6 @@ int cs3d_launch_count(cs3d_handle *h, long long *count);
 #define CS3D_OPT_STORE_INCREMENTS  1
 #define CS3D_OPT_STORE_DIAGNOSTICS 2
 #define CS3D_OPT_KERNEL_TIMING     3  /* bracket every launch with CUDA events */
-#define CS3D_OPT_SWEEP_PIPELINE    4  /* FP32-mixed z sweep: 1 (the default where
-                                         two tiles fit in shared memory) = one
-                                         persistent block per SM that solves
-                                         one tile while it streams the previous
-                                         and next; 0 = one block per tile.
-                                         Both give the same numbers bit for bit. */
 int cs3d_set_option(cs3d_handle *h, int option, int value);
 
 /* Kernel classes of cs3d_kernel_times. */

@@ -111,47 +111,3 @@ def test_mixed_rk4_accumulator_mid_step(gpu_pkg, cases):
     tol = 2e-7 * np.abs(dq4).max() + 1e-15 * np.abs(q2w).max()
     assert np.abs(q2n - (q2w + dq4 / 6)).max() <= tol
     s.close()
-
-
-@pytest.mark.parametrize("name", ["tgv32", "ragged", "wall_moving_sponge", "shear", "tgv128"])
-def test_pipelined_z_sweep_is_bitwise_the_one_tile_sweep(gpu_pkg, cases, name):
-    """The FP32-mixed z sweep pipelined across tiles (one persistent block per
-    SM, solve of one tile overlapped with the streaming phases of its
-    neighbours) gives the same numbers as one block per tile, bit for bit:
-    partial tiles (Nx not a multiple of 8), fewer tiles than SMs, walls,
-    moving walls and sponge faces, TVD-RK3, and the benchmark grid."""
-    abi = importlib.import_module("3dcompactsolver_gb300._abi")
-    mk = {
-        "tgv32": lambda: cases.tgv(32, precision=abi.FP32_MIXED),
-        "ragged": lambda: _ragged_mixed(cases, abi),
-        "wall_moving_sponge": lambda: cases.wall_box((20, 16, 12), moving=True, sponge=True,
-                                                     precision=abi.FP32_MIXED),
-        "shear": lambda: cases.shear_layer(64, 24, 42, precision=abi.FP32_MIXED),
-        "tgv128": lambda: cases.tgv(128, precision=abi.FP32_MIXED),
-    }[name]
-    out = []
-    for pipe in (1, 0):
-        cfg, ic = mk()
-        s = gpu_pkg.Solver(cfg)
-        s.set_option(gpu_pkg.OPT_SWEEP_PIPELINE, pipe)
-        s.set_initial_conditions(*ic)
-        s.run(6)
-        s.sync()
-        out.append((s.conserved(), s.scalars()))
-        s.close()
-    assert np.array_equal(out[0][0], out[1][0]), name
-    assert out[0][1] == out[1][1], name
-
-
-def _ragged_mixed(cases, abi):
-    cfg, _ = cases.tgv(8)
-    shape = (37, 11, 19)
-    cfg = abi.make_config(shape, (2.0, 1.7, 1.3), alphaF=0.48, mu_ref=1e-3, CFL=0.5, precision=abi.FP32_MIXED)
-    Nx, Ny, Nz = shape
-    z, y, x = np.meshgrid(np.linspace(0, 1.3, Nz), np.linspace(0, 1.7, Ny), np.linspace(0, 2, Nx), indexing="ij")
-    rho = 1 + 0.05 * np.sin(3 * x + 2 * y) * np.cos(z)
-    U = 0.2 * np.sin(2 * y) * np.cos(z)
-    V = 0.1 * np.cos(x + z)
-    W = 0.1 * np.sin(x - y)
-    p = np.full(x.shape, 1 / 1.4)
-    return cfg, (rho, p, U, V, W)
