@@ -363,6 +363,8 @@ struct cs3d_handle {
     std::vector<void *> adj_allocs, adj_rec_allocs;
     int adj_ws = 0;
     void *adj_tape[48] = {}, *adj_gbar[48] = {}, *adj_flux[15] = {};
+    void *adj_tapes[4][48] = {};  // the tapes of a step's four stages (set 0 is adj_tape)
+    void *tape_out[48] = {};      // where run_stage's sweeps write their tape (null: nowhere)
     double *adj_f[kAdjFields][5] = {};
     double *adj_part = nullptr;
     int adj_nsteps = 0, adj_every = 0;
@@ -887,6 +889,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
     a.sponge = h->sponge;
     a.sigma = h->sigma;
     a.savg = h->savg;
+    for (int i = 0; i < 48; i++) a.tape[i] = (T *)h->tape_out[i];
     for (int d = 0; d < 3; d++) {
         a.threads = h->threads[d];
         a.L = h->L[d];
@@ -1597,6 +1600,9 @@ static int adj_workspace(cs3d_handle *h) {
     for (int i = 0; i < 48; i++) {
         if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_tape[i], n * h->tb))) return rc;
         if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_gbar[i], n * h->tb))) return rc;
+        h->adj_tapes[0][i] = h->adj_tape[i];
+        for (int st = 1; st < 4; st++)
+            if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_tapes[st][i], n * h->tb))) return rc;
     }
     for (int i = 0; i < 15; i++)
         if ((rc = adj_alloc(h, h->adj_allocs, &h->adj_flux[i], n * h->tb))) return rc;
@@ -1615,10 +1621,11 @@ static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializ
     a.g = h->g;
     const int N = d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz;
     a.ntask = (int)tasks.size();
-    a.L = pick_L(sizeof(T), a.ntask, N, d == 0 ? 1 : 0);
+    const int nbuf = sizeof(T) == 4 ? 2 * ((a.ntask + 1) / 2) : a.ntask;
+    a.L = pick_L(sizeof(T), nbuf, N, d == 0 ? 1 : 0, 72, true);
     a.lgL = ilog2(a.L);
     a.P = a.L + (d == 0 ? 1 : 0);
-    a.threads = 128;
+    a.threads = apply_threads<T>();
     a.divN = make_fastdiv((unsigned)N);
     const DevOp<T> *ops = sizeof(T) == 8 ? reinterpret_cast<const DevOp<T> *>(h->op64[d])
                                          : reinterpret_cast<const DevOp<T> *>(h->op32[d]);
@@ -1626,6 +1633,19 @@ static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializ
     a.op1 = ops[kind1].op;
     int k = 0;
     for (const ApplyTask<T> &t : tasks) a.t[k++] = t;
+    // pairs (2i, 2i+1) that write one destination are merged; every other
+    // destination must occur once in the launch (the kernel reads each
+    // destination it adds to before any store)
+    std::vector<const void *> dsts;
+    for (int i = 0; i < a.ntask; i++) {
+        const bool second = (i & 1) && a.t[i].dst && a.t[i].dst == a.t[i - 1].dst;
+        if (second) a.merge[i / 2] = 1;
+        if (a.t[i].dst && !second) dsts.push_back(a.t[i].dst);
+        if (a.t[i].dst2) dsts.push_back(a.t[i].dst2);
+    }
+    for (size_t i = 0; i < dsts.size(); i++)
+        for (size_t j = i + 1; j < dsts.size(); j++)
+            if (dsts[i] == dsts[j]) return fail(CS3D_ERR_STATE, "adjoint operator launch with a repeated destination");
     tstart(h, CS3D_K_OTHER);
     CS3D_CUDA(launch_apply<T>(d, ops[kind0].op.H, a, h->stream));
     tend(h);
@@ -1679,12 +1699,13 @@ static int adj_tape(cs3d_handle *h, const T *const qin[5]) {
     return CS3D_OK;
 }
 
-// out = J(q)^T lam for the right-hand side R(q) of one stage
+// out = J(q)^T lam for the right-hand side R(q) of one stage whose tape
+// (primitives and derivative values at q) is G
 template <typename T>
-static int adj_rhs_vjp(cs3d_handle *h, const T *const qin[5], double *const lam[5], double *const out[5]) {
-    int rc = adj_tape<T>(h, qin);
-    if (rc) return rc;
-    T **G = reinterpret_cast<T **>(h->adj_tape);
+static int adj_vjp_tape(cs3d_handle *h, const T *const qin[5], void *const Gv[48], double *const lam[5],
+                        double *const out[5]) {
+    int rc;
+    T *const *G = reinterpret_cast<T *const *>(Gv);
     T **B = reinterpret_cast<T **>(h->adj_gbar);
     VjpArgs<T> va{};
     va.g = h->g;
@@ -1738,6 +1759,15 @@ static int adj_rhs_vjp(cs3d_handle *h, const T *const qin[5], double *const lam[
     CS3D_CUDA(launch_chain<T>(ca, h->stream));
     tend(h);
     return CS3D_OK;
+}
+
+// out = J(q)^T lam at a state q given on its own: the tape by the generic
+// line operators, then the transposed Jacobian
+template <typename T>
+static int adj_rhs_vjp(cs3d_handle *h, const T *const qin[5], double *const lam[5], double *const out[5]) {
+    int rc = adj_tape<T>(h, qin);
+    if (rc) return rc;
+    return adj_vjp_tape<T>(h, qin, h->adj_tape, lam, out);
 }
 
 // out = a x + b y + c z on five-field groups (y, z may be null)
@@ -1803,8 +1833,15 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     if ((rc = adj_set_state(h, q0))) return rc;
     for (int f = 0; f < 5; f++) yin[0][f] = sizeof(T) == 8 ? (const T *)q0[f] : (const T *)h->q1s[f];
     if ((rc = cs3d_pre_step(h))) return rc;
-    for (int st = 1; st <= 3; st++) {
-        if ((rc = run_stage<T>(h, st, 0))) return rc;
+    // the four stages again: their sweeps write the stage tapes (the values
+    // the stage's right-hand side was formed from), and stages 1-3 give the
+    // inputs y2, y3, y4 of the next
+    for (int st = 1; st <= 4; st++) {
+        for (int i = 0; i < 48; i++) h->tape_out[i] = h->adj_tapes[st - 1][i];
+        rc = run_stage<T>(h, st, 0);
+        for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
+        if (rc) return rc;
+        if (st == 4) break;
         for (int f = 0; f < 5; f++) {
             const void *src = sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f];
             CS3D_CUDA(cudaMemcpyAsync(Y[st - 1][f], src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
@@ -1838,7 +1875,7 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
         if (s == 3) rc = adj_lin(h, LAM, ca[s], QB2, 0.0, nullptr);
         else rc = adj_lin(h, LAM, ca[s], QB2, cb[s], YT);
         if (rc) return rc;
-        if ((rc = adj_rhs_vjp<T>(h, yin[s], LAM, YT))) return rc;
+        if ((rc = adj_vjp_tape<T>(h, yin[s], h->adj_tapes[s], LAM, YT))) return rc;
         if (s == 3) rc = copy5(h, YS, YT);
         else rc = adj_lin(h, YS, 1.0, YS, 1.0, YT);
         if (rc) return rc;

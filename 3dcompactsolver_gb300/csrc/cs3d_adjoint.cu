@@ -26,41 +26,93 @@ namespace cs3d {
 // ---------------------------------------------------------------------
 // line operators along DIR on XYZ-layout fields
 // ---------------------------------------------------------------------
+// Tasks 2i and 2i+1 share a solve pair; in FP32 the tile is pair-interleaved
+// (an odd last task pairs with a copy of itself in a spare buffer) and the
+// loads and stores run several points per thread in flight, as in the sweeps.
+// Destinations are read (where a task adds) together with the sources, so no
+// store waits on a load.
 template <typename T, int DIR, int H>
-__global__ void __launch_bounds__(128) k_apply(ApplyArgs<T> a) {
+__global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
+    constexpr bool kPair = sizeof(T) == 4;
+    constexpr int BL = kPair ? 4 : 2, BS = 2;  // points per thread in flight: loads, stores
     const int L = a.L, P = a.P;
     const Tile t = make_tile<DIR>(a.g, L);
     const int N = t.N, NL = N * L;
-    const int nt = a.ntask;
-    Smem<T> sm = smem_layout<T>(nt, L, P, N);
+    const int nt = a.ntask, np = (nt + 1) / 2;
+    const auto sm = SweepSmem<T>::at(smem_raw, kPair ? 2 * np : nt, L, P, N);
     __shared__ Task tasks[kApplyMax / 2];
-    if ((int)threadIdx.x < (nt + 1) / 2) {
+    if ((int)threadIdx.x < np) {
         const int i = 2 * threadIdx.x, j = min(i + 1, nt - 1);
         tasks[threadIdx.x] = Task{(signed char)i, (signed char)i, (signed char)a.t[i].op,
-                                  (signed char)j, (signed char)j, (signed char)a.t[j].op};
+                                  (signed char)(kPair ? i + 1 : j), (signed char)(kPair ? i + 1 : j),
+                                  (signed char)a.t[j].op};
     }
-    for (int p = threadIdx.x; p < NL; p += blockDim.x) {
-        const Pt pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
-        if (!pt.ok) continue;
-        for (int k = 0; k < nt; ++k) {
-            T v = a.t[k].src[pt.gi];
-            if (a.t[k].src2) v += a.t[k].src2[pt.gi];
-            sm.b(k)[pt.o] = v;
-        }
-    }
+    struct In { Pt pt; T v[kApplyMax]; };
+    batched<In, BL>(NL,
+        [&](In &in, int p) {
+            in.pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = in.pt.gi;
+#pragma unroll
+            for (int k = 0; k < kApplyMax; ++k) {
+                if (k >= nt) break;
+                T v = a.t[k].src[gi];
+                if (a.t[k].src2) v += a.t[k].src2[gi];
+                in.v[k] = v;
+            }
+        },
+        [&](In &in) {
+            if (!in.pt.ok) return;
+            const int o = in.pt.o;
+#pragma unroll
+            for (int k = 0; k < kApplyMax; k += 2) {
+                if (k >= nt) break;
+                if constexpr (kPair) put2(sm, k / 2, o, in.v[k], in.v[k + 1 < nt ? k + 1 : k]);
+                else {
+                    sm.at(k, o) = in.v[k];
+                    if (k + 1 < nt) sm.at(k + 1, o) = in.v[k + 1];
+                }
+            }
+        });
     __syncthreads();
-    run_tasks<T, H>(sm, tasks, (nt + 1) / 2, L, t.nlines, a.op0, a.op1);
+    run_sweep_tasks<H, 0>(sm, tasks, np, L, t.nlines, a.op0, a.op1, threadIdx.x, blockDim.x);
     __syncthreads();
-    for (int p = threadIdx.x; p < NL; p += blockDim.x) {
-        const Pt pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
-        if (!pt.ok) continue;
-        for (int k = 0; k < nt; ++k) {
-            const ApplyTask<T> &tk = a.t[k];
-            const T v = tk.scale * get(sm, k, pt, L, tk.op == 1 ? a.op1 : a.op0);
-            if (tk.dst) tk.dst[pt.gi] = tk.acc ? tk.dst[pt.gi] + v : v;
-            if (tk.dst2) tk.dst2[pt.gi] = tk.dst2[pt.gi] + v;
-        }
-    }
+    struct Out { Pt pt; T d[kApplyMax], d2[kApplyMax]; };
+    batched<Out, BS>(NL,
+        [&](Out &o, int p) {
+            o.pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = o.pt.gi;
+#pragma unroll
+            for (int k = 0; k < kApplyMax; ++k) {
+                if (k >= nt) break;
+                const ApplyTask<T> &tk = a.t[k];
+                const bool second = (k & 1) && a.merge[k / 2];
+                o.d[k] = (tk.dst && tk.acc && !second) ? tk.dst[gi] : T(0);
+                o.d2[k] = tk.dst2 ? tk.dst2[gi] : T(0);
+            }
+        },
+        [&](Out &o) {
+            if (!o.pt.ok) return;
+            const unsigned gi = o.pt.gi;
+            const int n = o.pt.n;
+#pragma unroll
+            for (int k = 0; k < kApplyMax; ++k) {
+                if (k >= nt) break;
+                const ApplyTask<T> &tk = a.t[k];
+                const LineOp<T> &op = tk.op == 1 ? a.op1 : a.op0;
+                const T z = op.periodic ? ldc(&op.z[n]) : T(0);
+                const T v = tk.scale * get1(sm, k, o.pt, L, z);
+                if ((k & 1) && a.merge[k / 2]) {
+                    // the pair's one destination: (first task's result) then this task
+                    const T r = tk.acc ? o.d[k - 1] + v : v;
+                    tk.dst[gi] = r;
+                } else if ((k & 1) == 0 && k + 1 < nt && a.merge[k / 2]) {
+                    o.d[k] = tk.acc ? o.d[k] + v : v;  // carried to task k + 1
+                } else if (tk.dst) {
+                    tk.dst[gi] = tk.acc ? o.d[k] + v : v;
+                }
+                if (tk.dst2) tk.dst2[gi] = o.d2[k] + v;
+            }
+        });
 }
 
 // ---------------------------------------------------------------------
@@ -246,7 +298,8 @@ template <typename T>
 cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s) {
     if (a.ntask < 1 || a.ntask > kApplyMax) return cudaErrorInvalidValue;
     const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
-    const size_t sm = planar_smem_bytes((int)sizeof(T), a.ntask, a.L, a.P, N);
+    const size_t sm = sweep_smem_bytes((int)sizeof(T), sizeof(T) == 4 ? 2 * ((a.ntask + 1) / 2) : a.ntask, a.L,
+                                       a.P, N);
     const int L = a.L;
     dim3 grid = dir == 0 ? dim3((a.g.Ny + L - 1) / L, a.g.Nz)
                          : dir == 1 ? dim3((a.g.Nx + L - 1) / L, a.g.Nz) : dim3((a.g.Nx + L - 1) / L, a.g.Ny);

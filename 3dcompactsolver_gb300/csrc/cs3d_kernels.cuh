@@ -77,6 +77,10 @@ struct SweepArgs {
     const double *sigma;
     Q5 savg;
     double *dq_out[5];  // increments dq (optional)
+    // optional tape of the stage (the discrete adjoint): the primitives
+    // U, V, W, T and the 44 derivative values of the right-hand side, in the
+    // order of cs3d_rhs_adjoint.cuh's kIn* indices; null = not written
+    T *tape[48];
 };
 
 template <typename T>
@@ -264,7 +268,15 @@ struct ApplyArgs {
     LineOp<T> op0, op1;
     int ntask;
     ApplyTask<T> t[kApplyMax];
+    // merge[i]: tasks 2i and 2i+1 write one destination (t[2i].dst), the
+    // second adding to the first's result; every other destination (dst and
+    // dst2) appears once per launch (the host checks)
+    signed char merge[kApplyMax / 2];
 };
+// Threads per block of k_apply: 256 in FP32 (pair-interleaved tiles, as the
+// sweeps), 128 in FP64 (the filter's solves use up to ~250 registers).
+template <typename T>
+__host__ __device__ constexpr int apply_threads() { return sizeof(T) == 4 ? 256 : 128; }
 // primitives U V W T and the 15 Euler fluxes of the state q, in the work type
 template <typename T>
 struct TapePrepArgs {

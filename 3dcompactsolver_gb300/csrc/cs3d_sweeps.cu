@@ -161,6 +161,13 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
             get2(sm, 5, p, L, zz.z1, zz.z1, f2, f3);
             const T f4 = get1(sm, XF4, p, L, zz.z1);
             a.dx[0][gi] = Ux; a.dx[1][gi] = Vx; a.dx[2][gi] = Wx; a.dx[3][gi] = Tx;
+            if (a.tape[0]) {  // the tape's x entries (kIn* 0..16)
+                T *const *g = a.tape;
+                g[0][gi] = U; g[1][gi] = V; g[2][gi] = W; g[3][gi] = Tt;
+                g[4][gi] = Ux; g[5][gi] = Vx; g[6][gi] = Wx; g[7][gi] = Tx;
+                g[8][gi] = Uxx; g[9][gi] = Vxx; g[10][gi] = Wxx; g[11][gi] = Txx;
+                g[12][gi] = cex; g[13][gi] = f1; g[14][gi] = f2; g[15][gi] = f3; g[16][gi] = f4;
+            }
             a.R[0][gi] = -cex;
             a.R[1][gi] = mu * (c43 * Uxx) - f1;
             a.R[2][gi] = mu * Vxx - f2;
@@ -246,6 +253,13 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
             get2(sm, 6, p, L, zz.z1, zz.z1, f2, f3);
             const T f4 = get1(sm, YF4, p, L, zz.z1);
             a.dy[0][gi] = Uy; a.dy[1][gi] = Vy; a.dy[2][gi] = Wy; a.dy[3][gi] = Ty;
+            if (a.tape[0]) {  // the tape's y entries (kIn* 17..31)
+                T *const *g = a.tape;
+                g[17][gi] = Uy; g[18][gi] = Vy; g[19][gi] = Wy; g[20][gi] = Ty;
+                g[21][gi] = Uyy; g[22][gi] = Vyy; g[23][gi] = Wyy; g[24][gi] = Tyy;
+                g[25][gi] = Uxy; g[26][gi] = Vxy; g[27][gi] = cey;
+                g[28][gi] = f1; g[29][gi] = f2; g[30][gi] = f3; g[31][gi] = f4;
+            }
             int i, j, k;
             coords<1>(t, p.l, p.n, i, j, k);
             const int wd = a.wall_faces ? wall_dir(faces_of(a.g, i, j, k) & a.wall_faces) : -1;
@@ -412,6 +426,13 @@ struct ZSweep {
                 const bool zero_mom = wd >= 0;
                 if (a.diag[0]) {  // derivative fields of the last stage, for diagnostics
                     a.diag[0][gi] = Uz; a.diag[1][gi] = Vz; a.diag[2][gi] = Wz;
+                }
+                if (a.tape[0]) {  // the tape's z entries (kIn* 32..47)
+                    T *const *g = a.tape;
+                    g[32][gi] = Uz; g[33][gi] = Vz; g[34][gi] = Wz; g[35][gi] = Tz;
+                    g[36][gi] = Uzz; g[37][gi] = Vzz; g[38][gi] = Wzz; g[39][gi] = Tzz;
+                    g[40][gi] = S; g[41][gi] = Wxz; g[42][gi] = Wyz; g[43][gi] = cez;
+                    g[44][gi] = f1; g[45][gi] = f2; g[46][gi] = f3; g[47][gi] = f4;
                 }
 #pragma unroll
                 for (int f = 0; f < 5; ++f) {
