@@ -1615,8 +1615,11 @@ static int adj_workspace(cs3d_handle *h) {
 }
 
 // one launch of k_apply along d: tasks {src, src2, dst, dst2, scale, op, acc}
+// (or, f64io, {.., src64, dst64}); operator kinds 0 d1, 1 d2, 2 filter, 3 the
+// FP32 filter correction F - I
 template <typename T>
-static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializer_list<ApplyTask<T>> tasks) {
+static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializer_list<ApplyTask<T>> tasks,
+                     int f64io = 0) {
     ApplyArgs<T> a{};
     a.g = h->g;
     const int N = d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz;
@@ -1629,8 +1632,13 @@ static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializ
     a.divN = make_fastdiv((unsigned)N);
     const DevOp<T> *ops = sizeof(T) == 8 ? reinterpret_cast<const DevOp<T> *>(h->op64[d])
                                          : reinterpret_cast<const DevOp<T> *>(h->op32[d]);
-    a.op0 = ops[kind0].op;
-    a.op1 = ops[kind1].op;
+    auto opk = [&](int kind) {
+        if (kind == 3) return *reinterpret_cast<const LineOp<T> *>(&h->op32fc[d].op);
+        return ops[kind].op;
+    };
+    a.op0 = opk(kind0);
+    a.op1 = opk(kind1);
+    a.f64io = f64io;
     int k = 0;
     for (const ApplyTask<T> &t : tasks) a.t[k++] = t;
     // pairs (2i, 2i+1) that write one destination are merged; every other
@@ -1642,12 +1650,13 @@ static int adj_apply(cs3d_handle *h, int d, int kind0, int kind1, std::initializ
         if (second) a.merge[i / 2] = 1;
         if (a.t[i].dst && !second) dsts.push_back(a.t[i].dst);
         if (a.t[i].dst2) dsts.push_back(a.t[i].dst2);
+        if (a.t[i].dst64) dsts.push_back(a.t[i].dst64);
     }
     for (size_t i = 0; i < dsts.size(); i++)
         for (size_t j = i + 1; j < dsts.size(); j++)
             if (dsts[i] == dsts[j]) return fail(CS3D_ERR_STATE, "adjoint operator launch with a repeated destination");
     tstart(h, CS3D_K_OTHER);
-    CS3D_CUDA(launch_apply<T>(d, ops[kind0].op.H, a, h->stream));
+    CS3D_CUDA(launch_apply<T>(d, a.op0.H, a, h->stream));
     tend(h);
     return CS3D_OK;
 }
@@ -1701,9 +1710,19 @@ static int adj_tape(cs3d_handle *h, const T *const qin[5]) {
 
 // out = J(q)^T lam for the right-hand side R(q) of one stage whose tape
 // (primitives and derivative values at q) is G
+// Optional fusions of the RK combination of the adjoint stage: the
+// cotangent lam = ca qb2 + cb yt formed inside the pointwise VJP (qb2 set;
+// yt optional), and acc = out (acc_set) or acc + out inside the chain rule.
+struct VjpFuse {
+    double *const *qb2 = nullptr, *const *yt = nullptr;
+    double ca = 0.0, cb = 0.0;
+    double *const *acc = nullptr;
+    int acc_set = 0;
+};
+
 template <typename T>
 static int adj_vjp_tape(cs3d_handle *h, const T *const qin[5], void *const Gv[48], double *const lam[5],
-                        double *const out[5]) {
+                        double *const out[5], const VjpFuse &fz = VjpFuse{}) {
     int rc;
     T *const *G = reinterpret_cast<T *const *>(Gv);
     T **B = reinterpret_cast<T **>(h->adj_gbar);
@@ -1714,46 +1733,73 @@ static int adj_vjp_tape(cs3d_handle *h, const T *const qin[5], void *const Gv[48
         va.tape[i] = G[i];
         va.gbar[i] = B[i];
     }
-    for (int f = 0; f < 5; f++) va.lam[f] = lam[f];
+    for (int f = 0; f < 5; f++) {
+        va.lam[f] = lam ? lam[f] : nullptr;
+        va.qb2[f] = fz.qb2 ? fz.qb2[f] : nullptr;
+        va.yt[f] = fz.yt ? fz.yt[f] : nullptr;
+    }
+    va.ca = fz.ca;
+    va.cb = fz.cb;
     tstart(h, CS3D_K_OTHER);
     CS3D_CUDA(launch_vjp<T>(va, h->stream));
     tend(h);
     // transposed operators, z then y then x: D1^T = -D1, D2^T = D2
-    const T m1 = T(-1), p1 = T(1);
-    auto derivsT = [&](int d, int b1, int b2) {
-        return adj_apply<T>(h, d, 0, 1,
-                            {{B[b1 + 0], nullptr, B[kInU], nullptr, m1, 0, 1}, {B[b2 + 0], nullptr, B[kInU], nullptr, p1, 1, 1},
-                             {B[b1 + 1], nullptr, B[kInV], nullptr, m1, 0, 1}, {B[b2 + 1], nullptr, B[kInV], nullptr, p1, 1, 1},
-                             {B[b1 + 2], nullptr, B[kInW], nullptr, m1, 0, 1}, {B[b2 + 2], nullptr, B[kInW], nullptr, p1, 1, 1},
-                             {B[b1 + 3], nullptr, B[kInT], nullptr, m1, 0, 1}, {B[b2 + 3], nullptr, B[kInT], nullptr, p1, 1, 1}});
-    };
-    if ((rc = derivsT(2, kInUz, kInUzz))) return rc;
-    if ((rc = adj_apply<T>(h, 2, 0, 1,
-                           {{B[kInS], nullptr, B[kInUx], B[kInVy], m1, 0, 1}, {B[kInWxz], nullptr, B[kInWx], nullptr, m1, 0, 1},
-                            {B[kInWyz], nullptr, B[kInWy], nullptr, m1, 0, 1}, {B[kInCEz], nullptr, B[kInCEz], nullptr, m1, 0, 0},
-                            {B[kInH1z], nullptr, B[kInH1z], nullptr, m1, 0, 0}, {B[kInH2z], nullptr, B[kInH2z], nullptr, m1, 0, 0},
-                            {B[kInH3z], nullptr, B[kInH3z], nullptr, m1, 0, 0}, {B[kInH4z], nullptr, B[kInH4z], nullptr, m1, 0, 0}})))
-        return rc;
-    if ((rc = derivsT(1, kInUy, kInUyy))) return rc;
-    if ((rc = adj_apply<T>(h, 1, 0, 1,
-                           {{B[kInUxy], nullptr, B[kInUx], nullptr, m1, 0, 1}, {B[kInVxy], nullptr, B[kInVx], nullptr, m1, 0, 1},
-                            {B[kInCEy], nullptr, B[kInCEy], nullptr, m1, 0, 0}, {B[kInG1y], nullptr, B[kInG1y], nullptr, m1, 0, 0},
-                            {B[kInG2y], nullptr, B[kInG2y], nullptr, m1, 0, 0}, {B[kInG3y], nullptr, B[kInG3y], nullptr, m1, 0, 0},
-                            {B[kInG4y], nullptr, B[kInG4y], nullptr, m1, 0, 0}})))
-        return rc;
-    if ((rc = derivsT(0, kInUx, kInUxx))) return rc;
-    if ((rc = adj_apply<T>(h, 0, 0, 1,
-                           {{B[kInCEx], nullptr, B[kInCEx], nullptr, m1, 0, 0}, {B[kInF1x], nullptr, B[kInF1x], nullptr, m1, 0, 0},
-                            {B[kInF2x], nullptr, B[kInF2x], nullptr, m1, 0, 0}, {B[kInF3x], nullptr, B[kInF3x], nullptr, m1, 0, 0},
-                            {B[kInF4x], nullptr, B[kInF4x], nullptr, m1, 0, 0}})))
-        return rc;
+    if constexpr (sizeof(T) == 4) {
+        // one transposed sweep per direction, in the forward sweeps' tile shapes
+        for (int d = 2; d >= 0; d--) {
+            TSweepArgs ta{};
+            ta.g = h->g;
+            ta.L = h->L[d];
+            ta.lgL = ilog2(h->L[d]);
+            ta.P = h->L[d] + (d == 0 ? 1 : 0);
+            ta.threads = h->threads[d];
+            ta.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
+            ta.d1 = h->op32[d][0].op;
+            ta.d2 = h->op32[d][1].op;
+            for (int q = 0; q < 48; q++) ta.gbar[q] = reinterpret_cast<float *>(B[q]);
+            tstart(h, CS3D_K_OTHER);
+            CS3D_CUDA(launch_tsweep(d, ta, h->stream));
+            tend(h);
+        }
+    } else {
+        const T m1 = T(-1), p1 = T(1);
+        auto derivsT = [&](int d, int b1, int b2) {
+            return adj_apply<T>(h, d, 0, 1,
+                                {{B[b1 + 0], nullptr, B[kInU], nullptr, m1, 0, 1}, {B[b2 + 0], nullptr, B[kInU], nullptr, p1, 1, 1},
+                                 {B[b1 + 1], nullptr, B[kInV], nullptr, m1, 0, 1}, {B[b2 + 1], nullptr, B[kInV], nullptr, p1, 1, 1},
+                                 {B[b1 + 2], nullptr, B[kInW], nullptr, m1, 0, 1}, {B[b2 + 2], nullptr, B[kInW], nullptr, p1, 1, 1},
+                                 {B[b1 + 3], nullptr, B[kInT], nullptr, m1, 0, 1}, {B[b2 + 3], nullptr, B[kInT], nullptr, p1, 1, 1}});
+        };
+        if ((rc = derivsT(2, kInUz, kInUzz))) return rc;
+        if ((rc = adj_apply<T>(h, 2, 0, 1,
+                               {{B[kInS], nullptr, B[kInUx], B[kInVy], m1, 0, 1}, {B[kInWxz], nullptr, B[kInWx], nullptr, m1, 0, 1},
+                                {B[kInWyz], nullptr, B[kInWy], nullptr, m1, 0, 1}, {B[kInCEz], nullptr, B[kInCEz], nullptr, m1, 0, 0},
+                                {B[kInH1z], nullptr, B[kInH1z], nullptr, m1, 0, 0}, {B[kInH2z], nullptr, B[kInH2z], nullptr, m1, 0, 0},
+                                {B[kInH3z], nullptr, B[kInH3z], nullptr, m1, 0, 0}, {B[kInH4z], nullptr, B[kInH4z], nullptr, m1, 0, 0}})))
+            return rc;
+        if ((rc = derivsT(1, kInUy, kInUyy))) return rc;
+        if ((rc = adj_apply<T>(h, 1, 0, 1,
+                               {{B[kInUxy], nullptr, B[kInUx], nullptr, m1, 0, 1}, {B[kInVxy], nullptr, B[kInVx], nullptr, m1, 0, 1},
+                                {B[kInCEy], nullptr, B[kInCEy], nullptr, m1, 0, 0}, {B[kInG1y], nullptr, B[kInG1y], nullptr, m1, 0, 0},
+                                {B[kInG2y], nullptr, B[kInG2y], nullptr, m1, 0, 0}, {B[kInG3y], nullptr, B[kInG3y], nullptr, m1, 0, 0},
+                                {B[kInG4y], nullptr, B[kInG4y], nullptr, m1, 0, 0}})))
+            return rc;
+        if ((rc = derivsT(0, kInUx, kInUxx))) return rc;
+        if ((rc = adj_apply<T>(h, 0, 0, 1,
+                               {{B[kInCEx], nullptr, B[kInCEx], nullptr, m1, 0, 0}, {B[kInF1x], nullptr, B[kInF1x], nullptr, m1, 0, 0},
+                                {B[kInF2x], nullptr, B[kInF2x], nullptr, m1, 0, 0}, {B[kInF3x], nullptr, B[kInF3x], nullptr, m1, 0, 0},
+                                {B[kInF4x], nullptr, B[kInF4x], nullptr, m1, 0, 0}})))
+            return rc;
+    }
     ChainArgs<T> ca{};
     ca.g = h->g;
     ca.gas = h->gas;
     for (int f = 0; f < 5; f++) {
         ca.qin[f] = qin[f];
         ca.out[f] = out[f];
+        ca.acc[f] = fz.acc ? fz.acc[f] : nullptr;
     }
+    ca.acc_set = fz.acc_set;
     for (int i = 0; i < 48; i++) ca.gbar[i] = B[i];
     tstart(h, CS3D_K_OTHER);
     CS3D_CUDA(launch_chain<T>(ca, h->stream));
@@ -1823,7 +1869,7 @@ template <typename T>
 static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     int rc;
     double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
-    double **QB = h->adj_f[ADJ_QB], **QB2 = h->adj_f[ADJ_QB2], **LAM = h->adj_f[ADJ_LAM];
+    double **QB = h->adj_f[ADJ_QB], **QB2 = h->adj_f[ADJ_QB2];
     double **YS = h->adj_f[ADJ_YS], **YT = h->adj_f[ADJ_YT];
     const size_t n = (size_t)h->g.npts;
     // stage inputs y1 = q0, y2, y3, y4 of the forward step, in T
@@ -1857,6 +1903,20 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
         filter_order(fts + 1, order);
         for (int pass = 2; pass >= 0; pass--) {
             const int d = order[pass];
+            if (sizeof(T) == 4) {
+                // mixed handle: F^T qbar = qbar + (F - I) qbar with the
+                // correction in FP32 and the sum in FP64, the form of the
+                // mixed forward filter
+                if ((rc = adj_apply<float>(h, d, 3, 3,
+                                           {{nullptr, nullptr, nullptr, nullptr, 1.f, 0, 0, QB2[0], QB2[0]},
+                                            {nullptr, nullptr, nullptr, nullptr, 1.f, 0, 0, QB2[1], QB2[1]},
+                                            {nullptr, nullptr, nullptr, nullptr, 1.f, 0, 0, QB2[2], QB2[2]},
+                                            {nullptr, nullptr, nullptr, nullptr, 1.f, 0, 0, QB2[3], QB2[3]},
+                                            {nullptr, nullptr, nullptr, nullptr, 1.f, 0, 0, QB2[4], QB2[4]}},
+                                           1)))
+                    return rc;
+                continue;
+            }
             if ((rc = adj_apply<double>(h, d, 2, 2,
                                         {{QB2[0], nullptr, QB2[0], nullptr, 1.0, 0, 0},
                                          {QB2[1], nullptr, QB2[1], nullptr, 1.0, 0, 0},
@@ -1871,14 +1931,17 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};  // weight of k_s in q+
     const double cb[4] = {dt / 2.0, dt / 2.0, dt, 0.0};             // weight of k_s in y_{s+1}
     for (int s = 3; s >= 0; s--) {
-        // lam_s = ca_s qbar+ + cb_s ybar_{s+1}
-        if (s == 3) rc = adj_lin(h, LAM, ca[s], QB2, 0.0, nullptr);
-        else rc = adj_lin(h, LAM, ca[s], QB2, cb[s], YT);
-        if (rc) return rc;
-        if ((rc = adj_vjp_tape<T>(h, yin[s], h->adj_tapes[s], LAM, YT))) return rc;
-        if (s == 3) rc = copy5(h, YS, YT);
-        else rc = adj_lin(h, YS, 1.0, YS, 1.0, YT);
-        if (rc) return rc;
+        // lam_s = ca_s qbar+ + cb_s ybar_{s+1} (formed in the VJP kernel);
+        // ybar_s = J(y_s)^T lam_s into YT, and YS = sum of the ybar_s (in the
+        // chain-rule kernel)
+        VjpFuse fz;
+        fz.qb2 = QB2;
+        fz.yt = s == 3 ? nullptr : YT;
+        fz.ca = ca[s];
+        fz.cb = cb[s];
+        fz.acc = YS;
+        fz.acc_set = s == 3;
+        if ((rc = adj_vjp_tape<T>(h, yin[s], h->adj_tapes[s], nullptr, YT, fz))) return rc;
     }
     return adj_lin(h, QB, 1.0, QB2, 1.0, YS);
 }

@@ -21,6 +21,10 @@
 #include "cs3d_tile.cuh"
 #include "cs3d_rhs_adjoint.cuh"
 
+#ifndef CS3D_TMINB_X
+#define CS3D_TMINB_X 3  // resident blocks per SM the transposed x sweep is compiled for
+#endif
+
 namespace cs3d {
 
 // ---------------------------------------------------------------------
@@ -31,7 +35,9 @@ namespace cs3d {
 // loads and stores run several points per thread in flight, as in the sweeps.
 // Destinations are read (where a task adds) together with the sources, so no
 // store waits on a load.
-template <typename T, int DIR, int H>
+// F64IO: every task reads an FP64 field (narrowed to T) and adds its result
+// into an FP64 field.
+template <typename T, int DIR, int H, bool F64IO = false>
 __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
     constexpr bool kPair = sizeof(T) == 4;
     constexpr int BL = kPair ? 4 : 2, BS = 2;  // points per thread in flight: loads, stores
@@ -55,9 +61,13 @@ __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
 #pragma unroll
             for (int k = 0; k < kApplyMax; ++k) {
                 if (k >= nt) break;
-                T v = a.t[k].src[gi];
-                if (a.t[k].src2) v += a.t[k].src2[gi];
-                in.v[k] = v;
+                if constexpr (F64IO) {
+                    in.v[k] = to_work<T>(a.t[k].src64[gi]);
+                } else {
+                    T v = a.t[k].src[gi];
+                    if (a.t[k].src2) v += a.t[k].src2[gi];
+                    in.v[k] = v;
+                }
             }
         },
         [&](In &in) {
@@ -66,7 +76,11 @@ __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
 #pragma unroll
             for (int k = 0; k < kApplyMax; k += 2) {
                 if (k >= nt) break;
-                if constexpr (kPair) put2(sm, k / 2, o, in.v[k], in.v[k + 1 < nt ? k + 1 : k]);
+                if constexpr (kPair) {
+                    // (an odd last task pairs with a copy of itself)
+                    const T second = k + 1 < kApplyMax && k + 1 < nt ? in.v[k + 1 < kApplyMax ? k + 1 : k] : in.v[k];
+                    put2(sm, k / 2, o, in.v[k], second);
+                }
                 else {
                     sm.at(k, o) = in.v[k];
                     if (k + 1 < nt) sm.at(k + 1, o) = in.v[k + 1];
@@ -76,6 +90,30 @@ __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
     __syncthreads();
     run_sweep_tasks<H, 0>(sm, tasks, np, L, t.nlines, a.op0, a.op1, threadIdx.x, blockDim.x);
     __syncthreads();
+    if constexpr (F64IO) {
+        struct Out64 { Pt pt; double e[kApplyMax]; };
+        batched<Out64, BS>(NL,
+            [&](Out64 &o, int p) {
+                o.pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+#pragma unroll
+                for (int k = 0; k < kApplyMax; ++k) {
+                    if (k >= nt) break;
+                    o.e[k] = a.t[k].dst64[o.pt.gi];
+                }
+            },
+            [&](Out64 &o) {
+                if (!o.pt.ok) return;
+#pragma unroll
+                for (int k = 0; k < kApplyMax; ++k) {
+                    if (k >= nt) break;
+                    const ApplyTask<T> &tk = a.t[k];
+                    const LineOp<T> &op = tk.op == 1 ? a.op1 : a.op0;
+                    const T z = op.periodic ? ldc(&op.z[o.pt.n]) : T(0);
+                    tk.dst64[o.pt.gi] = o.e[k] + to_f64(tk.scale * get1(sm, k, o.pt, L, z));
+                }
+            });
+        return;
+    }
     struct Out { Pt pt; T d[kApplyMax], d2[kApplyMax]; };
     batched<Out, BS>(NL,
         [&](Out &o, int p) {
@@ -111,6 +149,124 @@ __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
                     tk.dst[gi] = tk.acc ? o.d[k] + v : v;
                 }
                 if (tk.dst2) tk.dst2[gi] = o.d2[k] + v;
+            }
+        });
+}
+
+// ---------------------------------------------------------------------
+// transposed sweeps (FP32-mixed adjoint)
+// ---------------------------------------------------------------------
+// The transposed line operators of one direction in one launch, laid out as
+// the forward sweep of that direction: pair t holds two cotangent fields
+// (the 1st and 2nd derivative entries of U, V, W, T, then the 1st-derivative
+// entries two by two; an odd last pair repeats its field in a spare buffer),
+// solved with the forward operators; the consume phase applies the signs of
+// D1^T = -D1, D2^T = D2 and adds each result to its destination in the order
+// the tape's formulas used them.  Cotangent entries of the fluxes (CE, F/G/H)
+// are replaced in place; those of U, V, W, T and of the x/y derivatives that
+// a later direction differentiates (Ux, Vy, Wx, Wy from z; Ux, Vx from y) are
+// added to.
+__constant__ Task kTasksT[8] = {{0, 0, 0, 1, 1, 1}, {2, 2, 0, 3, 3, 1}, {4, 4, 0, 5, 5, 1}, {6, 6, 0, 7, 7, 1},
+                                {8, 8, 0, 9, 9, 0}, {10, 10, 0, 11, 11, 0}, {12, 12, 0, 13, 13, 0},
+                                {14, 14, 0, 15, 15, 0}};
+
+// cotangent entries solved along DIR, lane by lane (-1: the spare buffer)
+template <int DIR>
+struct TSweepSrc;
+template <>
+struct TSweepSrc<2> {
+    static constexpr int n = 16;
+    static __host__ __device__ constexpr int e(int k) {
+        constexpr int v[16] = {kInUz, kInUzz, kInVz,  kInVzz, kInWz,  kInWzz, kInTz,  kInTzz,
+                               kInS,  kInWxz, kInWyz, kInCEz, kInH1z, kInH2z, kInH3z, kInH4z};
+        return v[k];
+    }
+};
+template <>
+struct TSweepSrc<1> {
+    static constexpr int n = 15;
+    static __host__ __device__ constexpr int e(int k) {
+        constexpr int v[16] = {kInUy,  kInUyy, kInVy,  kInVyy, kInWy,  kInWyy, kInTy,  kInTyy,
+                               kInUxy, kInVxy, kInCEy, kInG1y, kInG2y, kInG3y, kInG4y, -1};
+        return v[k];
+    }
+};
+template <>
+struct TSweepSrc<0> {
+    static constexpr int n = 13;
+    static __host__ __device__ constexpr int e(int k) {
+        constexpr int v[16] = {kInUx,  kInUxx, kInVx,  kInVxx, kInWx, kInWxx, kInTx, kInTxx,
+                               kInCEx, kInF1x, kInF2x, kInF3x, kInF4x, -1,    -1,    -1};
+        return v[k];
+    }
+};
+
+template <int DIR, int PC>
+__global__ void __launch_bounds__(sweep_threads<float>(DIR), DIR == 0 ? CS3D_TMINB_X : 1) k_tsweep(TSweepArgs a) {
+    using S = TSweepSrc<DIR>;
+    constexpr int NP = (S::n + 1) / 2;
+    const int L = a.L, P = PC > 0 ? PC : a.P;
+    const Tile t = make_tile<DIR>(a.g, L);
+    const int N = t.N, NL = N * L;
+    const SmemPair sm = smem_pair_at(smem_raw, 2 * NP, L, P, N);
+    float *const *B = a.gbar;
+    struct In { Pt pt; float v[S::n]; };
+    batched<In, 4>(NL,
+        [&](In &in, int p) {
+            in.pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+#pragma unroll
+            for (int k = 0; k < S::n; ++k) in.v[k] = B[S::e(k)][in.pt.gi];
+        },
+        [&](In &in) {
+            if (!in.pt.ok) return;
+#pragma unroll
+            for (int q = 0; q < NP; ++q) put2(sm, q, in.pt.o, in.v[2 * q], in.v[2 * q + 1 < S::n ? 2 * q + 1 : 2 * q]);
+        });
+    __syncthreads();
+    run_sweep_tasks<2, PC>(sm, kTasksT, NP, L, t.nlines, a.d1, a.d2, threadIdx.x, blockDim.x);
+    __syncthreads();
+    // destinations added to: U V W T, then (z) Ux Vy Wx Wy / (y) Ux Vx
+    constexpr int ND = DIR == 2 ? 8 : DIR == 1 ? 6 : 4;
+    struct Out { Pt pt; float d[ND]; };
+    batched<Out, 2>(NL,
+        [&](Out &o, int p) {
+            o.pt = point<DIR>(t, p, L, P, a.lgL, a.divN);
+            const unsigned gi = o.pt.gi;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) o.d[f] = B[kInU + f][gi];
+            if constexpr (DIR == 2) {
+                o.d[4] = B[kInUx][gi]; o.d[5] = B[kInVy][gi]; o.d[6] = B[kInWx][gi]; o.d[7] = B[kInWy][gi];
+            } else if constexpr (DIR == 1) {
+                o.d[4] = B[kInUx][gi]; o.d[5] = B[kInVx][gi];
+            }
+        },
+        [&](Out &o) {
+            if (!o.pt.ok) return;
+            const Pt &p = o.pt;
+            const unsigned gi = p.gi;
+            const Zn<float> zz = zn(a.d1, a.d2, p.n);
+            float g[2 * NP];
+#pragma unroll
+            for (int q = 0; q < NP; ++q)
+                get2(sm, q, p, L, zz.z1, q < 4 ? zz.z2 : zz.z1, g[2 * q], g[2 * q + 1]);
+            // U V W T: (dst + (-D1 g_d)) + D2 g_dd
+#pragma unroll
+            for (int f = 0; f < 4; ++f) B[kInU + f][gi] = (o.d[f] + (-g[2 * f])) + g[2 * f + 1];
+            if constexpr (DIR == 2) {
+                B[kInUx][gi] = o.d[4] + (-g[8]);
+                B[kInVy][gi] = o.d[5] + (-g[8]);
+                B[kInWx][gi] = o.d[6] + (-g[9]);
+                B[kInWy][gi] = o.d[7] + (-g[10]);
+#pragma unroll
+                for (int k = 11; k < 16; ++k) B[S::e(k)][gi] = -g[k];
+            } else if constexpr (DIR == 1) {
+                B[kInUx][gi] = o.d[4] + (-g[8]);
+                B[kInVx][gi] = o.d[5] + (-g[9]);
+#pragma unroll
+                for (int k = 10; k < 15; ++k) B[S::e(k)][gi] = -g[k];
+            } else {
+#pragma unroll
+                for (int k = 8; k < 13; ++k) B[S::e(k)][gi] = -g[k];
             }
         });
 }
@@ -154,7 +310,15 @@ __global__ void __launch_bounds__(128) k_vjp(VjpArgs<T> a) {
 #pragma unroll
         for (int i = 0; i < kRhsIn; ++i) in[i] = a.tape[i][gi];
 #pragma unroll
-        for (int f = 0; f < 5; ++f) l[f] = (T)a.lam[f][gi];
+        for (int f = 0; f < 5; ++f) {
+            if (a.qb2[0]) {
+                double v = a.ca * a.qb2[f][gi];
+                if (a.yt[0]) v += a.cb * a.yt[f][gi];
+                l[f] = (T)v;
+            } else {
+                l[f] = (T)a.lam[f][gi];
+            }
+        }
         rhs_vjp<T>(in, l, muref, cpPr, out);
 #pragma unroll
         for (int i = 0; i < kRhsIn; ++i) a.gbar[i][gi] = out[i];
@@ -230,11 +394,12 @@ __global__ void k_chain(ChainArgs<T> a) {
         grv += gV * ir - gm1 * V * gp;
         grw += gW * ir - gm1 * W * gp;
         gre += gm1 * gp;
-        a.out[0][gi] = (double)gr;
-        a.out[1][gi] = (double)gru;
-        a.out[2][gi] = (double)grv;
-        a.out[3][gi] = (double)grw;
-        a.out[4][gi] = (double)gre;
+        const double o[5] = {(double)gr, (double)gru, (double)grv, (double)grw, (double)gre};
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            a.out[f][gi] = o[f];
+            if (a.acc[0]) a.acc[f][gi] = a.acc_set ? o[f] : a.acc[f][gi] + o[f];
+        }
     }
 }
 
@@ -303,6 +468,11 @@ cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s) 
     const int L = a.L;
     dim3 grid = dir == 0 ? dim3((a.g.Ny + L - 1) / L, a.g.Nz)
                          : dir == 1 ? dim3((a.g.Nx + L - 1) / L, a.g.Nz) : dim3((a.g.Nx + L - 1) / L, a.g.Ny);
+    if (H == 4 && a.f64io) {
+        if (dir == 0) return tile_launch(k_apply<T, 0, 4, true>, a, grid, sm, s);
+        if (dir == 1) return tile_launch(k_apply<T, 1, 4, true>, a, grid, sm, s);
+        return tile_launch(k_apply<T, 2, 4, true>, a, grid, sm, s);
+    }
     if (H == 4) {
         if (dir == 0) return tile_launch(k_apply<T, 0, 4>, a, grid, sm, s);
         if (dir == 1) return tile_launch(k_apply<T, 1, 4>, a, grid, sm, s);
@@ -311,6 +481,24 @@ cudaError_t launch_apply(int dir, int H, const ApplyArgs<T> &a, cudaStream_t s) 
     if (dir == 0) return tile_launch(k_apply<T, 0, 2>, a, grid, sm, s);
     if (dir == 1) return tile_launch(k_apply<T, 1, 2>, a, grid, sm, s);
     return tile_launch(k_apply<T, 2, 2>, a, grid, sm, s);
+}
+
+cudaError_t launch_tsweep(int dir, const TSweepArgs &a, cudaStream_t s) {
+    const int N = dir == 0 ? a.g.Nx : dir == 1 ? a.g.Ny : a.g.Nz;
+    const int nbuf = dir == 0 ? 14 : 16;
+    const size_t sm = sweep_smem_bytes(4, nbuf, a.L, a.P, N);
+    const int L = a.L;
+    dim3 grid = dir == 0 ? dim3((a.g.Ny + L - 1) / L, a.g.Nz)
+                         : dir == 1 ? dim3((a.g.Nx + L - 1) / L, a.g.Nz) : dim3((a.g.Nx + L - 1) / L, a.g.Ny);
+    if (dir == 0 && a.P == 9) return tile_launch(k_tsweep<0, 9>, a, grid, sm, s);
+    if (dir == 0 && a.P == 5) return tile_launch(k_tsweep<0, 5>, a, grid, sm, s);
+    if (dir == 1 && a.P == 16) return tile_launch(k_tsweep<1, 16>, a, grid, sm, s);
+    if (dir == 1 && a.P == 8) return tile_launch(k_tsweep<1, 8>, a, grid, sm, s);
+    if (dir == 2 && a.P == 16) return tile_launch(k_tsweep<2, 16>, a, grid, sm, s);
+    if (dir == 2 && a.P == 8) return tile_launch(k_tsweep<2, 8>, a, grid, sm, s);
+    if (dir == 0) return tile_launch(k_tsweep<0, 0>, a, grid, sm, s);
+    if (dir == 1) return tile_launch(k_tsweep<1, 0>, a, grid, sm, s);
+    return tile_launch(k_tsweep<2, 0>, a, grid, sm, s);
 }
 
 template <typename T>

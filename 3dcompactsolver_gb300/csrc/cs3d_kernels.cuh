@@ -259,6 +259,10 @@ struct ApplyTask {
     T scale;
     int op;   // 0: op0, 1: op1
     int acc;  // 1: dst += v, 0: dst = v
+    // FP64 in / FP64 accumulate (ApplyArgs::f64io): v = op(narrowed src64),
+    // dst64 += v in FP64 -- the FP32 correction form of a filter on an FP64 field
+    const double *src64;
+    double *dst64;
 };
 template <typename T>
 struct ApplyArgs {
@@ -272,6 +276,7 @@ struct ApplyArgs {
     // second adding to the first's result; every other destination (dst and
     // dst2) appears once per launch (the host checks)
     signed char merge[kApplyMax / 2];
+    int f64io;  // every task reads src64 and adds into dst64 (see ApplyTask)
 };
 // Threads per block of k_apply: 256 in FP32 (pair-interleaved tiles, as the
 // sweeps), 128 in FP64 (the filter's solves use up to ~250 registers).
@@ -292,8 +297,25 @@ struct VjpArgs {
     GasParams gas;
     const T *tape[48];
     const double *lam[5];
+    // instead of lam (qb2 set): lam = ca qb2 + cb yt, yt optional -- the RK
+    // weights of the adjoint stage, formed where they are used
+    const double *qb2[5], *yt[5];
+    double ca, cb;
     T *gbar[48];
 };
+// Transposed sweep of one direction (FP32-mixed adjoint): the direction's
+// 16 / 15 / 13 transposed line operators (D1^T = -D1, D2^T = D2) on the
+// cotangents of its derivative entries in gbar, accumulated into the
+// cotangents of the values they were taken of, with the sweeps' tile shapes.
+struct TSweepArgs {
+    Geom g;
+    int L, lgL, P, threads;
+    FastDiv divN;
+    LineOp<float> d1, d2;
+    float *gbar[48];  // cotangents, indexed as the tape (kIn* of cs3d_rhs_adjoint.cuh)
+};
+cudaError_t launch_tsweep(int dir, const TSweepArgs &a, cudaStream_t s);
+
 template <typename T>
 struct ChainArgs {
     Geom g;
@@ -301,6 +323,8 @@ struct ChainArgs {
     const T *qin[5];
     const T *gbar[48];
     double *out[5];
+    double *acc[5];  // optional: acc = out (acc_set) or acc + out
+    int acc_set;
 };
 template <typename T>
 struct RhsEvalArgs {
