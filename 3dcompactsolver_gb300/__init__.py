@@ -31,6 +31,7 @@ LIB_PATH = os.environ.get("CS3D_LIB_PATH") or os.path.join(HERE, "libcs3d_gb300.
 OPT_STORE_INCREMENTS = 1
 OPT_STORE_DIAGNOSTICS = 2
 OPT_KERNEL_TIMING = 3
+OPT_ADJ_RECOMPUTE = 4
 OP_DERIV1, OP_DERIV2, OP_FILTER = 1, 2, 3  # kinds of the operator-only handle
 ADJ_SEED = 0       # cs3d_adjoint_backward: dJ/dq of the final state given
 ADJ_KE_MEAN = 1    # J = mean over points of rho |u|^2 / 2 of the final state

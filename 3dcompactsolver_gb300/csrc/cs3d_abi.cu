@@ -371,6 +371,11 @@ struct cs3d_handle {
     std::vector<double *> adj_ckpt;  // 5*npts each: the state before step k*adj_every
     std::vector<int> adj_ts, adj_fts;
     double *adj_seg = nullptr;       // adj_every states of the segment being reversed
+    // segment mode (where the device has room): the tapes and stage inputs of
+    // every step of a segment, written while the segment is replayed, so the
+    // steps are not run a second time: [step][stage][48 tape / 5 input fields]
+    int adj_segmode = 0, adj_recompute = 0;
+    char *adj_segtape = nullptr, *adj_segyin = nullptr;
     int adj_end_ts = 0, adj_end_fts = 0;
     double adj_end_scal[2] = {0, 0};
 };
@@ -1194,6 +1199,8 @@ extern "C" int cs3d_set_option(cs3d_handle *h, int option, int value) {
         h->store_diag = value != 0;
     } else if (option == CS3D_OPT_KERNEL_TIMING) {
         h->timing = value != 0;
+    } else if (option == CS3D_OPT_ADJ_RECOMPUTE) {
+        h->adj_recompute = value != 0;
     } else {
         return fail(CS3D_ERR_ARG, "unknown option %d", option);
     }
@@ -1860,41 +1867,15 @@ static int adj_set_state(cs3d_handle *h, double *const q[5]) {
     return h->mixed ? launch_shadow_of(h, h->q1, h->q1s) : CS3D_OK;
 }
 
-// Adjoint of one time step taken from the state q0 with counters (ts, fts):
-// adj_f[ADJ_QB] holds dJ/dq after the step on entry and dJ/dq0 on return.
-// T is the work type: the stage Jacobians are transposed in T at the stage
-// inputs the forward used (FP64 q1, qk; or, in the mixed form, the FP32
-// shadows q1s, qks); the adjoint state and the filter transpose stay FP64.
+// The backward part of one time step from the state's filter step count fts
+// before it, whether it filtered, its stage inputs yin and its stage tapes:
+// adj_f[ADJ_QB] holds dJ/dq after the step on entry and dJ/dq before it on
+// return.
 template <typename T>
-static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
+static int adj_back(cs3d_handle *h, int fts, bool filtered, const T *const yin[4][5], void *const tapes[4][48]) {
     int rc;
-    double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
     double **QB = h->adj_f[ADJ_QB], **QB2 = h->adj_f[ADJ_QB2];
     double **YS = h->adj_f[ADJ_YS], **YT = h->adj_f[ADJ_YT];
-    const size_t n = (size_t)h->g.npts;
-    // stage inputs y1 = q0, y2, y3, y4 of the forward step, in T
-    const T *yin[4][5];
-    h->timeStep = ts;
-    h->filterTimeStep = fts;
-    if ((rc = adj_set_state(h, q0))) return rc;
-    for (int f = 0; f < 5; f++) yin[0][f] = sizeof(T) == 8 ? (const T *)q0[f] : (const T *)h->q1s[f];
-    if ((rc = cs3d_pre_step(h))) return rc;
-    // the four stages again: their sweeps write the stage tapes (the values
-    // the stage's right-hand side was formed from), and stages 1-3 give the
-    // inputs y2, y3, y4 of the next
-    for (int st = 1; st <= 4; st++) {
-        for (int i = 0; i < 48; i++) h->tape_out[i] = h->adj_tapes[st - 1][i];
-        rc = run_stage<T>(h, st, 0);
-        for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
-        if (rc) return rc;
-        if (st == 4) break;
-        for (int f = 0; f < 5; f++) {
-            const void *src = sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f];
-            CS3D_CUDA(cudaMemcpyAsync(Y[st - 1][f], src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
-            yin[st][f] = (const T *)Y[st - 1][f];
-        }
-    }
-    const bool filtered = h->timeStep % h->cfg.filter_step == 0;
     const double dt = h->cfg.dt_fixed;
     // the filter's transpose: F = F_o2 F_o1 F_o0, F^T = F_o0 F_o1 F_o2 (each symmetric)
     if ((rc = copy5(h, QB2, QB))) return rc;
@@ -1941,9 +1922,83 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
         fz.cb = cb[s];
         fz.acc = YS;
         fz.acc_set = s == 3;
-        if ((rc = adj_vjp_tape<T>(h, yin[s], h->adj_tapes[s], nullptr, YT, fz))) return rc;
+        if ((rc = adj_vjp_tape<T>(h, yin[s], tapes[s], nullptr, YT, fz))) return rc;
     }
     return adj_lin(h, QB, 1.0, QB2, 1.0, YS);
+}
+
+// Adjoint of one time step taken from the state q0 with counters (ts, fts):
+// the four stages run again with their sweeps writing the stage tapes, then
+// adj_back.  T is the work type: the stage Jacobians are transposed in T at
+// the stage inputs the forward used (FP64 q1, qk; or, in the mixed form, the
+// FP32 shadows q1s, qks); the adjoint state and the filter transpose stay FP64.
+template <typename T>
+static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
+    int rc;
+    double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
+    const size_t n = (size_t)h->g.npts;
+    // stage inputs y1 = q0, y2, y3, y4 of the forward step, in T
+    const T *yin[4][5];
+    h->timeStep = ts;
+    h->filterTimeStep = fts;
+    if ((rc = adj_set_state(h, q0))) return rc;
+    for (int f = 0; f < 5; f++) yin[0][f] = sizeof(T) == 8 ? (const T *)q0[f] : (const T *)h->q1s[f];
+    if ((rc = cs3d_pre_step(h))) return rc;
+    // the four stages again: their sweeps write the stage tapes (the values
+    // the stage's right-hand side was formed from), and stages 1-3 give the
+    // inputs y2, y3, y4 of the next
+    for (int st = 1; st <= 4; st++) {
+        for (int i = 0; i < 48; i++) h->tape_out[i] = h->adj_tapes[st - 1][i];
+        rc = run_stage<T>(h, st, 0);
+        for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
+        if (rc) return rc;
+        if (st == 4) break;
+        for (int f = 0; f < 5; f++) {
+            const void *src = sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f];
+            CS3D_CUDA(cudaMemcpyAsync(Y[st - 1][f], src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
+            yin[st][f] = (const T *)Y[st - 1][f];
+        }
+    }
+    const bool filtered = h->timeStep % h->cfg.filter_step == 0;
+    return adj_back<T>(h, fts, filtered, yin, h->adj_tapes);
+}
+
+// Segment mode: one full time step from the current state (as cs3d_step)
+// with the sweeps writing the tapes of its four stages, and the stage inputs
+// copied, into slot j of the segment storage.
+template <typename T>
+static int adj_taped_step(cs3d_handle *h, int j) {
+    int rc;
+    const size_t fb = (size_t)h->g.npts * sizeof(T);
+    if ((rc = cs3d_pre_step(h))) return rc;
+    for (int st = 1; st <= 4; st++) {
+        char *yb = h->adj_segyin + (size_t)((j * 4 + st - 1) * 5) * fb;
+        for (int f = 0; f < 5; f++) {
+            const void *src = st == 1 ? (sizeof(T) == 8 ? (const void *)h->q1.f[f] : (const void *)h->q1s[f])
+                                      : (sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f]);
+            CS3D_CUDA(cudaMemcpyAsync(yb + f * fb, src, fb, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        char *tb = h->adj_segtape + (size_t)((j * 4 + st - 1) * 48) * fb;
+        for (int i = 0; i < 48; i++) h->tape_out[i] = tb + i * fb;
+        rc = run_stage<T>(h, st, st == 4);
+        for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
+        if (rc) return rc;
+    }
+    return cs3d_post_step(h);
+}
+
+// Segment mode: the backward part of step j of the segment, from the storage.
+template <typename T>
+static int adj_back_stored(cs3d_handle *h, int j, int ts, int fts) {
+    const size_t fb = (size_t)h->g.npts * sizeof(T);
+    const T *yin[4][5];
+    void *tapes[4][48];
+    for (int st = 0; st < 4; st++) {
+        for (int f = 0; f < 5; f++)
+            yin[st][f] = reinterpret_cast<const T *>(h->adj_segyin + (size_t)((j * 4 + st) * 5 + f) * fb);
+        for (int i = 0; i < 48; i++) tapes[st][i] = h->adj_segtape + (size_t)((j * 4 + st) * 48 + i) * fb;
+    }
+    return adj_back<T>(h, fts, (ts + 1) % h->cfg.filter_step == 0, yin, tapes);
 }
 
 extern "C" int cs3d_adjoint_record(cs3d_handle *h, int nsteps, int checkpoint_every) {
@@ -1972,6 +2027,21 @@ extern "C" int cs3d_adjoint_record(cs3d_handle *h, int nsteps, int checkpoint_ev
         h->adj_ckpt.push_back((double *)p);
     }
     if ((rc = adj_alloc(h, h->adj_rec_allocs, (void **)&h->adj_seg, n5 * 8 * (size_t)every))) return rc;
+    // segment mode where the tapes and stage inputs of one segment (212 fields
+    // in the work precision per step) fit in half of the free device memory
+    h->adj_segmode = 0;
+    h->adj_segtape = h->adj_segyin = nullptr;
+    {
+        const size_t fb = (size_t)h->g.npts * h->tb;
+        const size_t tape_b = (size_t)every * 4 * 48 * fb, yin_b = (size_t)every * 4 * 5 * fb;
+        size_t free_b = 0, total_b = 0;
+        CS3D_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        if (!h->adj_recompute && tape_b + yin_b <= free_b / 2) {
+            if ((rc = adj_alloc(h, h->adj_rec_allocs, (void **)&h->adj_segtape, tape_b))) return rc;
+            if ((rc = adj_alloc(h, h->adj_rec_allocs, (void **)&h->adj_segyin, yin_b))) return rc;
+            h->adj_segmode = 1;
+        }
+    }
     for (int k = 0; k < nsteps; k++) {
         if (k % every == 0) {
             double *ck[5];
@@ -2040,6 +2110,27 @@ extern "C" int cs3d_adjoint_backward(cs3d_handle *h, int objective, const double
         if ((rc = copy5(h, st, ck))) return rc;
         h->timeStep = h->adj_ts[sg];
         h->filterTimeStep = h->adj_fts[sg];
+        if (h->adj_segmode) {
+            // replay the segment once, its steps keeping their tapes and stage
+            // inputs; then take the steps back from that storage.  Each step
+            // starts from its FP64 state, as in the per-step recompute.
+            for (int j = 0; j < m; j++) {
+                double *cur[5];
+                slab5(h, h->adj_seg, cur);
+                tsv[j] = h->timeStep;
+                ftsv[j] = h->filterTimeStep;
+                if ((rc = adj_set_state(h, cur))) return rc;
+                rc = h->mixed ? adj_taped_step<float>(h, j) : adj_taped_step<double>(h, j);
+                if (rc) return rc;
+                if (j + 1 < m && (rc = copy5(h, cur, h->q1.f))) return rc;
+            }
+            for (int j = m - 1; j >= 0; j--) {
+                rc = h->mixed ? adj_back_stored<float>(h, j, tsv[j], ftsv[j])
+                              : adj_back_stored<double>(h, j, tsv[j], ftsv[j]);
+                if (rc) return rc;
+            }
+            continue;
+        }
         for (int j = 0; j < m; j++) {
             tsv[j] = h->timeStep;
             ftsv[j] = h->filterTimeStep;

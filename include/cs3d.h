@@ -173,6 +173,7 @@ int cs3d_launch_count(cs3d_handle *h, long long *count);
 #define CS3D_OPT_STORE_INCREMENTS  1
 #define CS3D_OPT_STORE_DIAGNOSTICS 2
 #define CS3D_OPT_KERNEL_TIMING     3  /* bracket every launch with CUDA events */
+#define CS3D_OPT_ADJ_RECOMPUTE     4  /* adjoint: recompute each step's stages (see below) */
 int cs3d_set_option(cs3d_handle *h, int option, int value);
 
 /* Kernel classes of cs3d_kernel_times. */
@@ -304,8 +305,13 @@ int cs3d_load_solution(cs3d_handle *h, const char *prefix, int time_step, double
  * at every checkpoint_every-th step (0: ceil(sqrt(n))); memory is
  * (n/checkpoint_every + checkpoint_every) states plus a workspace of about
  * 150 fields.  cs3d_adjoint_backward replays each segment from its
- * checkpoint, recomputes the stage inputs of every step and takes the steps
- * back; it writes dJ/dq0 to grad (5*npts, field-major rho, rhoU, rhoV, rhoW,
+ * checkpoint and takes its steps back.  Where it fits in half of the free
+ * device memory at record time, the replay keeps the stage tapes and stage
+ * inputs of the whole segment (212 work-precision fields per step, e.g.
+ * 3.5 GB per step at 128^3 FP64), so that no step runs forward twice; else,
+ * or with CS3D_OPT_ADJ_RECOMPUTE on when cs3d_adjoint_record is called, each
+ * step's stages run again just before that step is taken back.  Both give the
+ * same bits.  cs3d_adjoint_backward writes dJ/dq0 to grad (5*npts, field-major rho, rhoU, rhoV, rhoW,
  * rhoE) and returns the solver to the recorded final state.  objective
  * CS3D_ADJ_KE_MEAN: J = mean over points of rho |u|^2 / 2 of the final
  * state (returned in *J); CS3D_ADJ_SEED: seed = dJ/dq of the final state

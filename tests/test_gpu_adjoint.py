@@ -9,7 +9,9 @@ FP64 forward (the same product path, fixed time step).
   velocity equals central differences of the forward on seeded random
   directions, filtered every step and every second step;
 * the checkpoint interval does not change the gradient, and the solver is
-  back at its recorded final state afterwards.
+  back at its recorded final state afterwards;
+* the backward from the tapes kept by the segment replay equals, bit for
+  bit, the one that recomputes each step's stages.
 """
 import numpy as np
 import pytest
@@ -120,6 +122,33 @@ def test_adjoint_checkpointing_and_restore(gpu_pkg, cases):
         ref.run(nsteps + 1)
         assert np.array_equal(s.conserved(), ref.conserved())
     assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_adjoint_segment_storage_equals_recompute(gpu_pkg, cases, mixed):
+    """The backward from the tapes and stage inputs kept by the segment replay
+    gives the same bits as the per-step recompute of each step's stages
+    (OPT_ADJ_RECOMPUTE): 7 steps in segments of 3 (one ragged), filter every
+    second step, FP64 and FP32-mixed handles."""
+    N, nsteps = 16, 7
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=2)
+    if mixed:
+        dt = cfg.dt_fixed
+        cfg, _ = cases.tgv(N, filter_step=2, precision=gpu_pkg.FP32_MIXED)
+        cfg.dt_fixed = dt
+    out = []
+    for recompute in (0, 1):
+        s = gpu_pkg.Solver(cfg)
+        s.set_initial_conditions(*ic)
+        s.set_option(gpu_pkg.OPT_ADJ_RECOMPUTE, recompute)
+        s.adjoint_record(nsteps, 3)
+        qN = s.conserved()
+        g, J = s.adjoint_backward(gpu_pkg.ADJ_KE_MEAN)
+        assert np.array_equal(s.conserved(), qN)
+        out.append((g, J))
+        s.close()
+    assert np.isfinite(out[0][0]).all() and np.abs(out[0][0]).max() > 0
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
 
 
 def test_adjoint_user_seed_is_linear(gpu_pkg, cases):
