@@ -75,8 +75,8 @@ namespace cs3d {
 // ---------------------------------------------------------------------
 // Sweep task t solves into buffers 2t and 2t+1.  The FP32-mixed form's pair
 // layout gives the last task of the x and y sweeps (one field) a spare second
-// buffer (XDUM, YDUM) that its second, duplicate solve writes; the FP64 form
-// solves that field twice over in its own buffer.
+// lane (XDUM, YDUM), which no thread solves; the FP64 form solves that field
+// twice over in its own buffer.
 enum { XU = 0, XU2, XV, XV2, XW, XW2, XT, XT2, XRU, XF1, XF2, XF3, XF4, XDUM, XNB2 };
 constexpr int XNB = XDUM;
 __constant__ Task kTasksX[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1}, {XW, XW, 0, XW, XW2, 1},
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MIN
         });
     __syncthreads();
     run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksX2 : kTasksX, 7, L, t.nlines, a.d1, a.d2, threadIdx.x,
-                           blockDim.x);
+                           blockDim.x, XDUM);
     __syncthreads();
     // phase C
     const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
         });
     __syncthreads();
     run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksY2 : kTasksY, 8, L, t.nlines, a.d1, a.d2, threadIdx.x,
-                           blockDim.x);
+                           blockDim.x, YDUM);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };

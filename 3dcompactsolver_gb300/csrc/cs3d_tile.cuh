@@ -259,46 +259,74 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
 }
 
 // ---------------------------------------------------------------------
-// paired FP32 line solves on pair-interleaved lines (the FP32-mixed sweeps)
+// FP32 line solves on pair-interleaved lines (the FP32-mixed sweeps)
 // ---------------------------------------------------------------------
 // The two solves of a task keep their lines pair-interleaved in shared
-// memory: element n of the pair is the float2 pr[n*P], lane x holding solve
-// A's line and lane y solve B's, so a row of both is one 64-bit load or
-// store.  Each solve reads its own lane and writes it in place (where both
-// solves differentiate one field, the load phase stores the field in both
-// lanes).  The arithmetic is per lane, the operations and their order those
-// of solve_pair, so the results are the same bit for bit.  (The packed f32x2
-// multiply-add was measured too: no faster than two scalar ones here.)
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
-}
-__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+// memory: element n of the pair is the float2 at row n, lane x holding solve
+// A's line and lane y solve B's.  Each solve reads its own lane and writes it
+// in place (where both solves differentiate one field, the load phase stores
+// the field in both lanes).  A task runs on two threads, one lane each
+// (NL = 1: a warp's 32 lanes read 16 lines x 2 lanes, 128 contiguous bytes a
+// row), or on one thread that takes both lanes with 64-bit accesses (NL = 2).
+// The arithmetic is per lane, the operations and their order those of
+// solve_pair, so every form gives the same bits.
+template <int NL>
+struct Lanes;
+template <>
+struct Lanes<2> {
+    using V = float2;
+    static __device__ __forceinline__ V mk(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ V fma_(V a, V b, V c) {
+        return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+    }
+    static __device__ __forceinline__ V mul(V a, V b) { return make_float2(a.x * b.x, a.y * b.y); }
+    static __device__ __forceinline__ float la(V v) { return v.x; }
+    static __device__ __forceinline__ float lb(V v) { return v.y; }
+};
+template <>
+struct Lanes<1> {
+    using V = float;
+    static __device__ __forceinline__ V mk(float a, float) { return a; }
+    static __device__ __forceinline__ V fma_(V a, V b, V c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+    static __device__ __forceinline__ float la(V v) { return v; }
+    static __device__ __forceinline__ float lb(V v) { return v; }
+};
 
-template <int H, int PC>
-__device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa, float *fa, const LineOp<float> &ob,
-                                            float *fb, int P_) {
+// NL = 2: pr is the pair (row stride P float2s), A = lane x with (oa, fa),
+// B = lane y with (ob, fb).  NL = 1: pr points at one lane's first element
+// (row stride 2P floats) and only (oa, fa) are used.
+template <int NL, int H, int PC>
+__device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const LineOp<float> &oa, float *fa,
+                                            const LineOp<float> &ob, float *fb, int P_) {
+    using Ls = Lanes<NL>;
+    using V = typename Ls::V;
     constexpr int W = 2 * H + 1;
-    const int P = PC > 0 ? PC : P_;
+    const int P = (PC > 0 ? PC : P_) * (3 - NL);  // row stride in V
     const int N = oa.N;
     const float *lx = reinterpret_cast<const float *>(pr);
     float pa[2 * H], pb[2 * H];
-    boundary_rows<float, H>(lx, 2 * P, oa, pa);
-    boundary_rows<float, H>(lx + 1, 2 * P, ob, pb);
-    float2 t2[W];
+    boundary_rows<float, H>(lx, 2 * (PC > 0 ? PC : P_), oa, pa);
+    if constexpr (NL == 2) boundary_rows<float, H>(lx + 1, 2 * P, ob, pb);
+    else {
 #pragma unroll
-    for (int k = 0; k < W; ++k) t2[k] = make_float2(oa.taps[kMaxH - H + k], ob.taps[kMaxH - H + k]);
+        for (int b = 0; b < 2 * H; ++b) pb[b] = pa[b];
+    }
+    V t2[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) t2[k] = Ls::mk(oa.taps[kMaxH - H + k], ob.taps[kMaxH - H + k]);
     const float *__restrict__ ma = oa.m;
     const float *__restrict__ mb = ob.m;
     // window of the first interior row H: positions 0..2H
-    float2 w[W];
+    V w[W];
 #pragma unroll
     for (int k = 0; k < W; ++k) w[k] = pr[k * P];
     // rows 0..H-1
-    float2 y = make_float2(pa[0], pb[0]);
+    V y = Ls::mk(pa[0], pb[0]);
     pr[0] = y;
 #pragma unroll
     for (int n = 1; n < H; ++n) {
-        y = ffma2(make_float2(-ldc(&ma[n]), -ldc(&mb[n])), y, make_float2(pa[n], pb[n]));
+        y = Ls::fma_(Ls::mk(-ldc(&ma[n]), -ldc(&mb[n])), y, Ls::mk(pa[n], pb[n]));
         pr[n * P] = y;
     }
     // interior rows H..N-H-1 in chunks of kU (as solve_pair: chunks inside
@@ -307,8 +335,8 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
     int n = H;
     const int klo = max(oa.klo, ob.klo), khi = min(oa.khi, ob.khi);
     const int clo = H + kU * ((max(klo - H, 0) + kU - 1) / kU);
-    const float2 km2 = make_float2(-oa.km, -ob.km);
-    float2 nx[kU];
+    const V km2 = Ls::mk(-oa.km, -ob.km);
+    V nx[kU];
 #pragma unroll
     for (int j = 0; j < kU; ++j) nx[j] = pr[(n + H + 1 + j) * P];
     float ma4[kU], mb4[kU];
@@ -316,11 +344,11 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
     load4(ob.mf, mb4);
     auto fwd_chunk = [&](auto kconst) {
         constexpr bool K = decltype(kconst)::value;
-        float2 c[kU], mc[kU];
+        V c[kU], mc[kU];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
             c[j] = nx[j];
-            mc[j] = K ? km2 : make_float2(-ma4[j], -mb4[j]);
+            mc[j] = K ? km2 : Ls::mk(-ma4[j], -mb4[j]);
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) nx[j] = pr[(n + kU + H + 1 + j) * P];
@@ -328,17 +356,17 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
             load4(oa.mf + (n + kU - H), ma4);
             load4(ob.mf + (n + kU - H), mb4);
         }
-        float2 e[W + kU];
+        V e[W + kU];
 #pragma unroll
         for (int k = 0; k < W; ++k) e[k] = w[k];
 #pragma unroll
         for (int j = 0; j < kU; ++j) e[W + j] = c[j];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
-            float2 acc = make_float2(0.f, 0.f);
+            V acc = Ls::mk(0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < W; ++k) acc = ffma2(t2[k], e[j + k], acc);
-            y = ffma2(mc[j], y, acc);
+            for (int k = 0; k < W; ++k) acc = Ls::fma_(t2[k], e[j + k], acc);
+            y = Ls::fma_(mc[j], y, acc);
             pr[(n + j) * P] = y;
         }
 #pragma unroll
@@ -354,21 +382,21 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
 #pragma unroll 2
     for (; n + kU <= nend; n += kU) fwd_chunk(std::false_type{});
     for (; n < nend; ++n) {
-        float2 acc = make_float2(0.f, 0.f);
+        V acc = Ls::mk(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < W; ++k) acc = ffma2(t2[k], w[k], acc);
-        y = ffma2(make_float2(-ldc(&ma[n]), -ldc(&mb[n])), y, acc);
+        for (int k = 0; k < W; ++k) acc = Ls::fma_(t2[k], w[k], acc);
+        y = Ls::fma_(Ls::mk(-ldc(&ma[n]), -ldc(&mb[n])), y, acc);
 #pragma unroll
         for (int k = 0; k < W - 1; ++k) w[k] = w[k + 1];
         const int pos = n + H + 1;
-        w[W - 1] = pos < N ? pr[pos * P] : make_float2(0.f, 0.f);
+        w[W - 1] = pos < N ? pr[pos * P] : Ls::mk(0.f, 0.f);
         pr[n * P] = y;
     }
     // rows N-H..N-1
 #pragma unroll
     for (int b = 0; b < H; ++b) {
         const int r = N - H + b;
-        y = ffma2(make_float2(-ldc(&ma[r]), -ldc(&mb[r])), y, make_float2(pa[H + b], pb[H + b]));
+        y = Ls::fma_(Ls::mk(-ldc(&ma[r]), -ldc(&mb[r])), y, Ls::mk(pa[H + b], pb[H + b]));
         pr[r * P] = y;
     }
     // back substitution in chunks of kU, next chunk prefetched
@@ -376,25 +404,25 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
     const float *__restrict__ cb_ = ob.c;
     const float *__restrict__ ia = oa.iw;
     const float *__restrict__ ib = ob.iw;
-    float2 x = fmul2(y, make_float2(ldc(&ia[N - 1]), ldc(&ib[N - 1])));
+    V x = Ls::mul(y, Ls::mk(ldc(&ia[N - 1]), ldc(&ib[N - 1])));
     pr[(N - 1) * P] = x;
-    const float2 xl = x;
+    const V xl = x;
     n = N - 2;
-    float2 y4[kU];
+    V y4[kU];
 #pragma unroll
     for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - j, 0) * P];
     float cA[kU], cB[kU], iA[kU], iB[kU];
     load4(oa.cbk, cA); load4(ob.cbk, cB);
     load4(oa.ibk, iA); load4(ob.ibk, iB);
-    const float2 kc2 = make_float2(-oa.kc, -ob.kc), ki2 = make_float2(oa.kiw, ob.kiw);
+    const V kc2 = Ls::mk(-oa.kc, -ob.kc), ki2 = Ls::mk(oa.kiw, ob.kiw);
     auto bwd_chunk = [&](auto kconst) {
         constexpr bool K = decltype(kconst)::value;
-        float2 y0[kU], c0[kU], i0[kU];
+        V y0[kU], c0[kU], i0[kU];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
             y0[j] = y4[j];
-            c0[j] = K ? kc2 : make_float2(-cA[j], -cB[j]);
-            i0[j] = K ? ki2 : make_float2(iA[j], iB[j]);
+            c0[j] = K ? kc2 : Ls::mk(-cA[j], -cB[j]);
+            i0[j] = K ? ki2 : Ls::mk(iA[j], iB[j]);
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - kU - j, 0) * P];
@@ -405,7 +433,7 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
         }
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
-            x = fmul2(ffma2(c0[j], x, y0[j]), i0[j]);
+            x = Ls::mul(Ls::fma_(c0[j], x, y0[j]), i0[j]);
             pr[(n - j) * P] = x;
         }
     };
@@ -420,12 +448,13 @@ __device__ __forceinline__ void solve_pair2(float2 *pr, const LineOp<float> &oa,
 #pragma unroll 2
     for (; n - kU + 1 >= 0; n -= kU) bwd_chunk(std::false_type{});
     for (; n >= 0; --n) {
-        x = fmul2(ffma2(make_float2(-ldc(&ca_[n]), -ldc(&cb_[n])), x, pr[n * P]),
-                  make_float2(ldc(&ia[n]), ldc(&ib[n])));
+        x = Ls::mul(Ls::fma_(Ls::mk(-ldc(&ca_[n]), -ldc(&cb_[n])), x, pr[n * P]),
+                    Ls::mk(ldc(&ia[n]), ldc(&ib[n])));
         pr[n * P] = x;
     }
-    *fa = oa.periodic ? (float)((to_f64(x.x) + oa.bog * to_f64(xl.x)) * oa.inv_den) : 0.f;
-    *fb = ob.periodic ? (float)((to_f64(x.y) + ob.bog * to_f64(xl.y)) * ob.inv_den) : 0.f;
+    *fa = oa.periodic ? (float)((to_f64(Ls::la(x)) + oa.bog * to_f64(Ls::la(xl))) * oa.inv_den) : 0.f;
+    if constexpr (NL == 2)
+        *fb = ob.periodic ? (float)((to_f64(Ls::lb(x)) + ob.bog * to_f64(Ls::lb(xl))) * ob.inv_den) : 0.f;
 }
 
 // Row n of the explicit right-hand side of a line read from src (stride P):
@@ -821,25 +850,30 @@ __device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, 
 }
 
 // The tasks of a sweep tile; sweep task t solves into buffers 2t and 2t+1.
-// FP32-mixed: paired solves on the pair-interleaved layout; FP64: solve_pair
-// on the planar layout.
+// FP32-mixed: one lane of the pair-interleaved layout per thread, the lane
+// whose destination buffer is `skip` (a task's unused duplicate) left out;
+// FP64: solve_pair on the planar layout.
 template <int H, int PC>
 __device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *tasks, int ntask, int L, int nlines,
                                                 const LineOp<float> &op0, const LineOp<float> &op1, int tid,
-                                                int nthr) {
-    for (int w = tid; w < ntask * L; w += nthr) {
-        const int t = w / L, l = w - t * L;
+                                                int nthr, int skip = -1) {
+    for (int w = tid; w < 2 * ntask * L; w += nthr) {
+        // w = (task, line, lane), lane fastest: a warp holds 16 (task, line)
+        // pairs' two lanes
+        const int lane = w & 1, tl = w >> 1;
+        const int t = tl / L, l = tl - t * L;
         if (l >= nlines) continue;
         const Task tk = tasks[t];
-        const LineOp<float> &oa = tk.oa == 1 ? op1 : op0;
-        const LineOp<float> &ob = tk.ob == 1 ? op1 : op0;
-        solve_pair2<H, PC>(sm.pair(tk.da >> 1) + l, oa, &sm.fact[tk.da * L + l], ob, &sm.fact[tk.db * L + l], sm.P);
+        const int op = lane ? tk.ob : tk.oa, dst = lane ? tk.db : tk.da;
+        if (dst == skip) continue;
+        solve_lanes<1, H, PC>(reinterpret_cast<float *>(sm.pair(tk.da >> 1) + l) + lane, op == 1 ? op1 : op0,
+                              &sm.fact[dst * L + l], op0, nullptr, sm.P);
     }
 }
 template <int H, int PC>
 __device__ __forceinline__ void run_sweep_tasks(const Smem<double> &sm, const Task *tasks, int ntask, int L,
                                                 int nlines, const LineOp<double> &op0, const LineOp<double> &op1,
-                                                int tid, int nthr) {
+                                                int tid, int nthr, int = -1) {
     run_tasks<double, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, tid, nthr);
 }
 
