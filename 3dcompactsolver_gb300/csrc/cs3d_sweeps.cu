@@ -657,10 +657,16 @@ static size_t tile_smem(int nbuf, int L, int P, int N) {
 }
 
 // The FP32-mixed sweeps' pair-interleaved tiles: the per-line factors, then
-// (nbuf + 1) / 2 pair arrays.
+// (nbuf + 1) / 2 pair arrays of N rows each, then kPad rows of padding.  A
+// solve's read-ahead past its line's end (up to kU + 1 rows, values never
+// used) lands in the next pair array, or in the padding after the last one;
+// no per-array padding, so that the mixed tiles fit the next-smaller shared
+// memory carveout and leave L1 -- where the phases' global loads in flight
+// are held -- more room (128^3: y and z 138.8 -> 133.4 kB a block, x
+// 3 x 68.1 -> 3 x 65.8 kB).
 static size_t pair_tile_smem(int nbuf, int L, int P, int N) {
     const int nf = (nbuf * L + 3) & ~3;
-    return 4 * ((size_t)nf + (size_t)((nbuf + 1) / 2) * pair_stride(N + kPad, P));
+    return 4 * ((size_t)nf + (size_t)((nbuf + 1) / 2) * pair_stride(N, P) + (size_t)2 * kPad * P);
 }
 
 size_t planar_smem_bytes(int prec_bytes, int nbuf, int L, int P, int N) {

@@ -669,9 +669,10 @@ struct Smem {
 
 // Pair-interleaved layout of the FP32-mixed sweep tiles: buffers 2t and
 // 2t+1 (the two solves of task t) share one float2 array, element (n, l) of
-// the pair at float2 index n*P + l; pairs pstride floats apart, pstride = 16
-// (mod 32) so that the two tasks of a half-warp's 64-bit accesses cover
-// distinct banks.  Per-line factors stay planar: fact[k*L + l].
+// the pair at float2 index n*P + l; pairs pstride floats apart with no rows
+// of padding between them, pstride = 16 (mod 32) so that a warp whose
+// one-lane solves span two tasks (tiles of 8 lines) covers distinct banks.
+// Per-line factors stay planar: fact[k*L + l].
 struct SmemPair {
     float *buf;
     float *fact;
@@ -715,7 +716,7 @@ extern __shared__ __align__(16) unsigned char smem_raw[];
 __device__ __forceinline__ SmemPair smem_pair_at(unsigned char *base, int nbuf, int L, int P, int N) {
     SmemPair s;
     s.P = P;
-    s.pstride = pair_stride(N + kPad, P);
+    s.pstride = pair_stride(N, P);
     s.fact = reinterpret_cast<float *>(base);
     const int nf = (nbuf * L + 3) & ~3;
     s.buf = reinterpret_cast<float *>(base) + nf;
