@@ -35,19 +35,8 @@ def _deps():
     return out
 
 
-STAMP = os.path.join(OBJDIR, "flags.txt")
-
-
-def _extra():
-    """Extra nvcc flags from $CS3D_NVCC_EXTRA (tuning experiments)."""
-    return os.environ.get("CS3D_NVCC_EXTRA", "").split()
-
-
 def up_to_date():
     if not os.path.exists(LIB):
-        return False
-    flags = " ".join(_extra())
-    if not os.path.exists(STAMP) or open(STAMP).read() != flags:
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps())
@@ -62,7 +51,7 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc] + ARCH + FLAGS + _extra() + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
@@ -78,8 +67,6 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
     os.replace(tmp, LIB)
-    with open(STAMP, "w") as f:
-        f.write(" ".join(_extra()))
     return LIB
 
 

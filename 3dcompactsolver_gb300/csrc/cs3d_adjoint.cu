@@ -21,11 +21,9 @@
 #include "cs3d_tile.cuh"
 #include "cs3d_rhs_adjoint.cuh"
 
-#ifndef CS3D_TMINB_X
-#define CS3D_TMINB_X 3  // resident blocks per SM the transposed x sweep is compiled for
-#endif
-
 namespace cs3d {
+
+constexpr int kTMinBlocksX = 3;  // resident blocks per SM the transposed x sweep is compiled for
 
 // ---------------------------------------------------------------------
 // line operators along DIR on XYZ-layout fields
@@ -202,7 +200,7 @@ struct TSweepSrc<0> {
 };
 
 template <int DIR, int PC>
-__global__ void __launch_bounds__(sweep_threads<float>(DIR), DIR == 0 ? CS3D_TMINB_X : 1) k_tsweep(TSweepArgs a) {
+__global__ void __launch_bounds__(sweep_threads<float>(DIR), DIR == 0 ? kTMinBlocksX : 1) k_tsweep(TSweepArgs a) {
     using S = TSweepSrc<DIR>;
     constexpr int NP = (S::n + 1) / 2;
     const int L = a.L, P = PC > 0 ? PC : a.P;

@@ -2,14 +2,11 @@
 #pragma once
 #include "cs3d_dev.cuh"
 
-#ifndef CS3D_TPB_X
-#define CS3D_TPB_X 256   // threads per block of the mixed-form x sweep
-#endif
-#ifndef CS3D_TPB_YZ
-#define CS3D_TPB_YZ 512  // most threads per block of the mixed-form y and z sweeps
-#endif
-
 namespace cs3d {
+
+constexpr int kTpbX = 256;   // threads per block of the mixed-form x sweep
+constexpr int kTpbYZ = 512;  // most threads per block of the mixed-form y and z sweeps
+constexpr int kFilterTpb = 256;  // threads per block of the mixed-form filter
 
 // Most threads per block the stage sweeps in work type T, direction dir, are
 // compiled for.  The mixed-form x sweep (80 registers) runs 3 blocks of 256
@@ -18,14 +15,11 @@ namespace cs3d {
 // The plain FP64 form needs up to 255 registers per thread and runs 128.
 template <typename T>
 __host__ __device__ constexpr int sweep_threads(int dir) {
-    return sizeof(T) == 4 ? (dir == 0 ? CS3D_TPB_X : CS3D_TPB_YZ) : 128;
+    return sizeof(T) == 4 ? (dir == 0 ? kTpbX : kTpbYZ) : 128;
 }
 
-#ifndef CS3D_FTPB
-#define CS3D_FTPB 256  // threads per block of the mixed-form filter
-#endif
 template <typename T>
-__host__ __device__ constexpr int filter_threads() { return sizeof(T) == 4 ? CS3D_FTPB : 128; }
+__host__ __device__ constexpr int filter_threads() { return sizeof(T) == 4 ? kFilterTpb : 128; }
 
 // Ideal-gas constants (IdealGas.hpp:36-46).
 struct GasParams {

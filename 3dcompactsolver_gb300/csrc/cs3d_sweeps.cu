@@ -35,35 +35,20 @@
 #include <cmath>
 #include "cs3d_tile.cuh"
 
-#ifndef CS3D_FB
-#define CS3D_FB 4      // points per thread in flight in the mixed filter's load and store loops
-#endif
-#ifndef CS3D_FBC
-#define CS3D_FBC 2     // points per thread in flight in the mixed filter's consume loop
-#endif
-#ifndef CS3D_FMINB
-#define CS3D_FMINB 4   // resident blocks per SM the mixed filter is compiled for (64 registers)
-#endif
-#ifndef CS3D_YC
-#define CS3D_YC 4      // points per thread in flight in the y sweep's consume phase
-#endif
-#ifndef CS3D_ZC2
-#define CS3D_ZC2 2     // points per thread in flight in the z sweep's RK-update pass
-#endif
-// Resident blocks per SM the mixed-form sweeps are compiled for: x at 3
-// blocks of 256 threads (80 registers), y and z at one block of 512 (128
-// registers); the plain form runs 128 threads, 2 blocks.
-#ifndef CS3D_MINB_X
-#define CS3D_MINB_X 3
-#endif
-#ifndef CS3D_MINB_Y
-#define CS3D_MINB_Y 1
-#endif
-#ifndef CS3D_MINB_Z
-#define CS3D_MINB_Z 1
-#endif
-
 namespace cs3d {
+
+// Points per thread in flight in the point loops of the mixed form (measured
+// at 128^3 and 256^3; deeper batches spill or run no faster).
+constexpr int kFilterBatch = 4;         // the mixed filter's load and store loops
+constexpr int kFilterConsumeBatch = 2;  // the mixed filter's consume loop
+constexpr int kYConsumeBatch = 4;       // the y sweep's consume phase
+constexpr int kZUpdateBatch = 2;        // the z sweep's RK-update pass
+// Resident blocks per SM the mixed-form kernels are compiled for: the filter
+// at 4 (64 registers), the x sweep at 3 blocks of 256 threads (80 registers),
+// y and z at one block of 512 (128 registers); the plain form runs 128
+// threads, 2 blocks.
+constexpr int kFilterMinBlocks = 4;
+constexpr int kMinBlocksX = 3, kMinBlocksY = 1, kMinBlocksZ = 1;
 
 // The sweep kernels take the shared-memory pitch of their tile as a template
 // parameter PC (0: read at run time).  The launcher instantiates the mixed
@@ -87,7 +72,7 @@ __constant__ Task kTasksX2[7] = {{XU, XU, 0, XU, XU2, 1}, {XV, XV, 0, XV, XV2, 1
                                  {XF2, XF2, 0, XF3, XF3, 0}, {XF4, XF4, 0, XF4, XDUM, 0}};
 
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? CS3D_MINB_X : 2) k_sweep_x(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? kMinBlocksX : 2) k_sweep_x(SweepArgs<T> a) {
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<0>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -191,7 +176,7 @@ __constant__ Task kTasksY2[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1
                                  {YF4, YF4, 0, YF4, YDUM, 0}};
 
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MINB_Y : 2) k_sweep_y(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? kMinBlocksY : 2) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -228,7 +213,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? CS3D_MIN
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
-    batched<InC, sizeof(T) == 4 ? CS3D_YC : 2>(NL,
+    batched<InC, sizeof(T) == 4 ? kYConsumeBatch : 2>(NL,
         [&](InC &in, int p) {
             in.pt = point<1>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
@@ -448,7 +433,7 @@ struct ZSweep {
             double qa[5], qb[5];
             T qsv[5];    // q1's shadow: the stage input qs on stage 1, q1s on 2-3
         };
-        batched<InC2, CS3D_ZC2>(NL, tid, nthr,
+        batched<InC2, kZUpdateBatch>(NL, tid, nthr,
             [&](InC2 &in, int p) {
                 in.pt = point<2>(t, p, L, P, a.lgL, a.divN);
                 const unsigned gi = in.pt.gi;
@@ -513,7 +498,7 @@ struct ZSweep {
 };
 
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MINB_Z : 2) k_sweep_z(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? kMinBlocksZ : 2) k_sweep_z(SweepArgs<T> a) {
     const Tile t = make_tile<2>(a.g, a.L);
     const auto sm = SweepSmem<T>::at(smem_raw, ZNB, a.L, PC > 0 ? PC : a.P, t.N);
     ZSweep<T, PC>::load(a, t, sm, threadIdx.x, blockDim.x);
@@ -537,8 +522,8 @@ __global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? CS3D_MIN
 __constant__ Task kTasksF[3] = {{0, 0, 2, 1, 1, 2}, {2, 2, 2, 3, 3, 2}, {4, 4, 2, 4, 4, 2}};
 
 template <typename T, int DIR, int PC>
-__global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMINB : 4) k_filter(FilterArgs<T> a) {
-    constexpr int B = sizeof(T) == 4 ? CS3D_FB : 2;
+__global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? kFilterMinBlocks : 4) k_filter(FilterArgs<T> a) {
+    constexpr int B = sizeof(T) == 4 ? kFilterBatch : 2;
     constexpr bool kCorr = sizeof(T) == 4;
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<DIR>(a.g, L);
@@ -577,7 +562,7 @@ __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? CS3D_FMI
         run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
     }
     __syncthreads();
-    constexpr int BC = sizeof(T) == 4 ? CS3D_FBC : 2;
+    constexpr int BC = sizeof(T) == 4 ? kFilterConsumeBatch : 2;
     for (int p0 = threadIdx.x; p0 < NL; p0 += BC * blockDim.x) {
         Pt pt[BC];
         double q[BC][5];

@@ -15,10 +15,7 @@ constexpr int kU = 4;  // rows per unrolled chunk
 // Rows of padding after each line buffer in shared memory, so that the
 // chunked forward pass may read ahead past the line's end without a test:
 // it reads rows up to max(2H + kU, N + kU) = N + kU for N >= 8.
-#ifndef CS3D_KPAD
-#define CS3D_KPAD (kU + 2)
-#endif
-constexpr int kPad = CS3D_KPAD;
+constexpr int kPad = kU + 2;
 
 // The first H and last H rows of the right-hand side, from explicit rows.
 template <typename T, int H>
