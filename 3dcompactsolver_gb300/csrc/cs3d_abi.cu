@@ -267,7 +267,9 @@ int upload_op(const HostOp &h, DevOp<T> &d, cudaStream_t s) {
         int lo = mid, hi = mid + 1;
         while (lo > 1 && same(lo - 1)) --lo;
         while (hi < N - 1 && same(hi)) ++hi;
-        o.klo = lo;
+        // at least kU: a chunk of the back substitution inside the run then
+        // reads ahead no row below 0
+        o.klo = std::max(lo, kU);
         o.khi = hi;
     }
     o.km = (T)h.m[N / 2];

@@ -20,6 +20,8 @@ constexpr int kTaps = 2 * kMaxH + 1;
 //   forward   y_0 = r_0,  y_n = r_n - m_n y_{n-1}
 //   backward  x_{N-1} = y_{N-1} iw_{N-1},  x_n = (y_n - c_n x_{n+1}) iw_n
 //   cyclic    x_n -= f z_n,   f = (x_0 + bog x_{N-1}) inv_den   (f in FP64)
+constexpr int kU = 4;  // rows per unrolled chunk of the line solves
+
 template <typename T>
 struct LineOp {
     const T *m;          // forward multipliers a_n / w_{n-1}        [N]
@@ -33,7 +35,7 @@ struct LineOp {
     T btaps[2 * kMaxH][kTaps]; // the first H and last H rows, explicit
     int boff[2 * kMaxH]; // first column of each boundary row
     T scale;             // 1/h, 1/h^2 or 1
-    // Rows [klo, khi) (1 <= klo <= khi <= N-1) where m, iw and c equal km,
+    // Rows [klo, khi) (kU <= klo, khi <= N-1) where m, iw and c equal km,
     // kiw, kc bit for bit in T: the factors of the Toeplitz interior converge
     // geometrically, and there the recurrences run on register constants.
     T km, kiw, kc;

@@ -11,7 +11,6 @@ namespace cs3d {
 // ---------------------------------------------------------------------
 // line solves
 // ---------------------------------------------------------------------
-constexpr int kU = 4;  // rows per unrolled chunk
 // Rows of padding after each line buffer in shared memory, so that the
 // chunked forward pass may read ahead past the line's end without a test:
 // it reads rows up to max(2H + kU, N + kU) = N + kU for N >= 8.
@@ -421,8 +420,9 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
             c0[j] = K ? kc2 : Ls::mk(-cA[j], -cB[j]);
             i0[j] = K ? ki2 : Ls::mk(iA[j], iB[j]);
         }
+        // (inside [klo, khi), klo >= kU: the rows read ahead are >= 0)
 #pragma unroll
-        for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - kU - j, 0) * P];
+        for (int j = 0; j < kU; ++j) y4[j] = pr[(K ? n - kU - j : max(n - kU - j, 0)) * P];
         if (!K) {
             const int kb = N - 2 - (n - kU);
             load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
@@ -864,8 +864,10 @@ __device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *
         const Task tk = tasks[t];
         const int op = lane ? tk.ob : tk.oa, dst = lane ? tk.db : tk.da;
         if (dst == skip) continue;
+        // the other operator passed as B: its rows bound [klo, khi) too, so
+        // both lanes of a task (one warp) leave the constant-factor run together
         solve_lanes<1, H, PC>(reinterpret_cast<float *>(sm.pair(tk.da >> 1) + l) + lane, op == 1 ? op1 : op0,
-                              &sm.fact[dst * L + l], op0, nullptr, sm.P);
+                              &sm.fact[dst * L + l], op == 1 ? op0 : op1, nullptr, sm.P);
     }
 }
 template <int H, int PC>
