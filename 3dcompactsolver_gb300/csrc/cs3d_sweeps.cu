@@ -115,8 +115,8 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? kMinBloc
             put1(sm, 6, o, s.re * ss.U + ss.U * ss.p);
         });
     __syncthreads();
-    run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksX2 : kTasksX, 7, L, t.nlines, a.d1, a.d2, threadIdx.x,
-                           blockDim.x, XDUM);
+    run_sweep_solves<2, PC>(sm, sizeof(T) == 4 ? kTasksX2 : kTasksX, 7, L, t.nlines, a.d1, a.d2, threadIdx.x,
+                            blockDim.x, XDUM);
     __syncthreads();
     // phase C
     const T c43 = T(4.0 / 3.0), cpPr = (T)gp.cpPr, muref = (T)gp.mu_ref;
@@ -208,8 +208,8 @@ __global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? kMinBloc
             put1(sm, 7, o, re * V + V * pp);
         });
     __syncthreads();
-    run_sweep_tasks<2, PC>(sm, sizeof(T) == 4 ? kTasksY2 : kTasksY, 8, L, t.nlines, a.d1, a.d2, threadIdx.x,
-                           blockDim.x, YDUM);
+    run_sweep_solves<2, PC>(sm, sizeof(T) == 4 ? kTasksY2 : kTasksY, 8, L, t.nlines, a.d1, a.d2, threadIdx.x,
+                            blockDim.x, YDUM);
     __syncthreads();
     const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0), cpPr = (T)a.gas.cpPr;
     struct InC { Pt pt; T v[9]; };
@@ -309,7 +309,7 @@ struct ZSweep {
     // B: the 16 solves (8 pairs) of every line of the tile
     static __device__ __forceinline__ void solve(const SweepArgs<T> &a, const Tile &t, const SM &sm, int tid,
                                                  int nthr) {
-        run_sweep_tasks<2, PC>(sm, kTasksZ, 8, a.L, t.nlines, a.d1, a.d2, tid, nthr);
+        run_sweep_solves<2, PC>(sm, kTasksZ, 8, a.L, t.nlines, a.d1, a.d2, tid, nthr, -1);
     }
     // C: right-hand side, dq and the RK update of every point of the tile
     static __device__ __forceinline__ void consume(const SweepArgs<T> &a, const Tile &t, const SM &sm, int tid,
@@ -559,7 +559,8 @@ __global__ void __launch_bounds__(filter_threads<T>(), sizeof(T) == 4 ? kFilterM
             thomas_inplace<T, PC>(sm.b(5 + f) + l, a.op, &sm.fact[(5 + f) * L + l], P);
         }
     } else {
-        run_tasks<T, 4>(sm, kTasksF, 3, L, t.nlines, a.op, a.op);
+        // plain form: one solve per thread, each field in place
+        run_sweep_solves<4, 0>(sm, kTasksF, 3, L, t.nlines, a.op, a.op, (int)threadIdx.x, (int)blockDim.x);
     }
     __syncthreads();
     constexpr int BC = sizeof(T) == 4 ? kFilterConsumeBatch : 2;

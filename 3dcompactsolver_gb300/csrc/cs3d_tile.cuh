@@ -266,10 +266,10 @@ __device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &
 // row), or on one thread that takes both lanes with 64-bit accesses (NL = 2).
 // The arithmetic is per lane, the operations and their order those of
 // solve_pair, so every form gives the same bits.
-template <int NL>
+template <int NL, typename S = float>
 struct Lanes;
 template <>
-struct Lanes<2> {
+struct Lanes<2, float> {
     using V = float2;
     static __device__ __forceinline__ V mk(float a, float b) { return make_float2(a, b); }
     static __device__ __forceinline__ V fma_(V a, V b, V c) {
@@ -279,31 +279,33 @@ struct Lanes<2> {
     static __device__ __forceinline__ float la(V v) { return v.x; }
     static __device__ __forceinline__ float lb(V v) { return v.y; }
 };
-template <>
-struct Lanes<1> {
-    using V = float;
-    static __device__ __forceinline__ V mk(float a, float) { return a; }
-    static __device__ __forceinline__ V fma_(V a, V b, V c) { return fmaf(a, b, c); }
+template <typename S>
+struct Lanes<1, S> {
+    using V = S;
+    static __device__ __forceinline__ V mk(S a, S) { return a; }
+    static __device__ __forceinline__ V fma_(V a, V b, V c) { return fma(a, b, c); }
     static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
-    static __device__ __forceinline__ float la(V v) { return v; }
-    static __device__ __forceinline__ float lb(V v) { return v; }
+    static __device__ __forceinline__ S la(V v) { return v; }
+    static __device__ __forceinline__ S lb(V v) { return v; }
 };
 
 // NL = 2: pr is the pair (row stride P float2s), A = lane x with (oa, fa),
-// B = lane y with (ob, fb).  NL = 1: pr points at one lane's first element
-// (row stride 2P floats) and only (oa, fa) are used.
-template <int NL, int H, int PC>
-__device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const LineOp<float> &oa, float *fa,
-                                            const LineOp<float> &ob, float *fb, int P_) {
-    using Ls = Lanes<NL>;
+// B = lane y with (ob, fb).  NL = 1: pr points at one solve's first element,
+// row stride RS * P elements of type S (RS = 2: one lane of a pair array;
+// RS = 1: a planar buffer), and only (oa, fa) are used -- ob bounds the
+// constant-factor rows with oa.
+template <int NL, int H, int PC, typename S = float, int RS = 2>
+__device__ __forceinline__ void solve_lanes(typename Lanes<NL, S>::V *pr, const LineOp<S> &oa, S *fa,
+                                            const LineOp<S> &ob, S *fb, int P_) {
+    using Ls = Lanes<NL, S>;
     using V = typename Ls::V;
     constexpr int W = 2 * H + 1;
-    const int P = (PC > 0 ? PC : P_) * (3 - NL);  // row stride in V
+    const int P = (PC > 0 ? PC : P_) * (NL == 2 ? 1 : RS);  // row stride in V
     const int N = oa.N;
-    const float *lx = reinterpret_cast<const float *>(pr);
-    float pa[2 * H], pb[2 * H];
-    boundary_rows<float, H>(lx, 2 * (PC > 0 ? PC : P_), oa, pa);
-    if constexpr (NL == 2) boundary_rows<float, H>(lx + 1, 2 * P, ob, pb);
+    const S *lx = reinterpret_cast<const S *>(pr);
+    S pa[2 * H], pb[2 * H];
+    boundary_rows<S, H>(lx, NL == 2 ? 2 * P : P, oa, pa);
+    if constexpr (NL == 2) boundary_rows<S, H>(lx + 1, 2 * P, ob, pb);
     else {
 #pragma unroll
         for (int b = 0; b < 2 * H; ++b) pb[b] = pa[b];
@@ -311,8 +313,8 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
     V t2[W];
 #pragma unroll
     for (int k = 0; k < W; ++k) t2[k] = Ls::mk(oa.taps[kMaxH - H + k], ob.taps[kMaxH - H + k]);
-    const float *__restrict__ ma = oa.m;
-    const float *__restrict__ mb = ob.m;
+    const S *__restrict__ ma = oa.m;
+    const S *__restrict__ mb = ob.m;
     // window of the first interior row H: positions 0..2H
     V w[W];
 #pragma unroll
@@ -335,7 +337,7 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
     V nx[kU];
 #pragma unroll
     for (int j = 0; j < kU; ++j) nx[j] = pr[(n + H + 1 + j) * P];
-    float ma4[kU], mb4[kU];
+    S ma4[kU], mb4[kU];
     load4(oa.mf, ma4);
     load4(ob.mf, mb4);
     auto fwd_chunk = [&](auto kconst) {
@@ -359,7 +361,7 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
         for (int j = 0; j < kU; ++j) e[W + j] = c[j];
 #pragma unroll
         for (int j = 0; j < kU; ++j) {
-            V acc = Ls::mk(0.f, 0.f);
+            V acc = Ls::mk(S(0), S(0));
 #pragma unroll
             for (int k = 0; k < W; ++k) acc = Ls::fma_(t2[k], e[j + k], acc);
             y = Ls::fma_(mc[j], y, acc);
@@ -378,14 +380,14 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
 #pragma unroll 2
     for (; n + kU <= nend; n += kU) fwd_chunk(std::false_type{});
     for (; n < nend; ++n) {
-        V acc = Ls::mk(0.f, 0.f);
+        V acc = Ls::mk(S(0), S(0));
 #pragma unroll
         for (int k = 0; k < W; ++k) acc = Ls::fma_(t2[k], w[k], acc);
         y = Ls::fma_(Ls::mk(-ldc(&ma[n]), -ldc(&mb[n])), y, acc);
 #pragma unroll
         for (int k = 0; k < W - 1; ++k) w[k] = w[k + 1];
         const int pos = n + H + 1;
-        w[W - 1] = pos < N ? pr[pos * P] : Ls::mk(0.f, 0.f);
+        w[W - 1] = pos < N ? pr[pos * P] : Ls::mk(S(0), S(0));
         pr[n * P] = y;
     }
     // rows N-H..N-1
@@ -396,10 +398,10 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
         pr[r * P] = y;
     }
     // back substitution in chunks of kU, next chunk prefetched
-    const float *__restrict__ ca_ = oa.c;
-    const float *__restrict__ cb_ = ob.c;
-    const float *__restrict__ ia = oa.iw;
-    const float *__restrict__ ib = ob.iw;
+    const S *__restrict__ ca_ = oa.c;
+    const S *__restrict__ cb_ = ob.c;
+    const S *__restrict__ ia = oa.iw;
+    const S *__restrict__ ib = ob.iw;
     V x = Ls::mul(y, Ls::mk(ldc(&ia[N - 1]), ldc(&ib[N - 1])));
     pr[(N - 1) * P] = x;
     const V xl = x;
@@ -407,7 +409,7 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
     V y4[kU];
 #pragma unroll
     for (int j = 0; j < kU; ++j) y4[j] = pr[max(n - j, 0) * P];
-    float cA[kU], cB[kU], iA[kU], iB[kU];
+    S cA[kU], cB[kU], iA[kU], iB[kU];
     load4(oa.cbk, cA); load4(ob.cbk, cB);
     load4(oa.ibk, iA); load4(ob.ibk, iB);
     const V kc2 = Ls::mk(-oa.kc, -ob.kc), ki2 = Ls::mk(oa.kiw, ob.kiw);
@@ -449,9 +451,9 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL>::V *pr, const Lin
                     Ls::mk(ldc(&ia[n]), ldc(&ib[n])));
         pr[n * P] = x;
     }
-    *fa = oa.periodic ? (float)((to_f64(Ls::la(x)) + oa.bog * to_f64(Ls::la(xl))) * oa.inv_den) : 0.f;
+    *fa = oa.periodic ? (S)((to_f64(Ls::la(x)) + oa.bog * to_f64(Ls::la(xl))) * oa.inv_den) : S(0);
     if constexpr (NL == 2)
-        *fb = ob.periodic ? (float)((to_f64(Ls::lb(x)) + ob.bog * to_f64(Ls::lb(xl))) * ob.inv_den) : 0.f;
+        *fb = ob.periodic ? (S)((to_f64(Ls::lb(x)) + ob.bog * to_f64(Ls::lb(xl))) * ob.inv_den) : S(0);
 }
 
 // Row n of the explicit right-hand side of a line read from src (stride P):
@@ -660,6 +662,7 @@ struct Smem {
     T *fact;  // [nbuf][L]
     int bstride;
     int P;
+    int nbuf;
     __device__ T *b(int k) const { return buf + (size_t)k * bstride; }
     __device__ T &at(int k, int o) const { return buf[(size_t)k * bstride + o]; }
 };
@@ -701,6 +704,7 @@ template <typename T>
 __device__ __forceinline__ Smem<T> smem_layout_at(unsigned char *base, int nbuf, int L, int P, int N) {
     Smem<T> s;
     s.P = P;
+    s.nbuf = nbuf;
     s.bstride = buf_stride(N + kPad, P, L, (int)(sizeof(T) / 4));
     s.fact = reinterpret_cast<T *>(base);
     const int nf = (nbuf * L + 3) & ~3;
@@ -866,9 +870,36 @@ __device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *
         if (dst == skip) continue;
         // the other operator passed as B: its rows bound [klo, khi) too, so
         // both lanes of a task (one warp) leave the constant-factor run together
-        solve_lanes<1, H, PC>(reinterpret_cast<float *>(sm.pair(tk.da >> 1) + l) + lane, op == 1 ? op1 : op0,
-                              &sm.fact[dst * L + l], op == 1 ? op0 : op1, nullptr, sm.P);
+        solve_lanes<1, H, PC, float, 2>(reinterpret_cast<float *>(sm.pair(tk.da >> 1) + l) + lane,
+                                        op == 1 ? op1 : op0, &sm.fact[dst * L + l], op == 1 ? op0 : op1, nullptr,
+                                        sm.P);
     }
+}
+// The plain FP64 sweeps' solves: one solve per thread, in place in its
+// destination buffer (the load phase stores a field whose two solves read it
+// in both of its task's buffers), the duplicate solve of a one-field task
+// left out; the arithmetic of solve_pair, so the same bits.  The mixed form
+// is run_sweep_tasks.
+template <int H, int PC>
+__device__ __forceinline__ void run_sweep_solves(const Smem<double> &sm, const Task *tasks, int ntask, int L,
+                                                 int nlines, const LineOp<double> &op0, const LineOp<double> &op1,
+                                                 int tid, int nthr, int = -1) {
+    for (int w = tid; w < 2 * ntask * L; w += nthr) {
+        const int lane = w & 1, tl = w >> 1;
+        const int t = tl / L, l = tl - t * L;
+        if (l >= nlines) continue;
+        const Task tk = tasks[t];
+        if (lane && tk.db == tk.da) continue;
+        const int op = lane ? tk.ob : tk.oa, dst = lane ? tk.db : tk.da;
+        solve_lanes<1, H, PC, double, 1>(sm.b(dst) + l, op == 1 ? op1 : op0, &sm.fact[dst * L + l],
+                                         op == 1 ? op0 : op1, nullptr, sm.P);
+    }
+}
+template <int H, int PC>
+__device__ __forceinline__ void run_sweep_solves(const SmemPair &sm, const Task *tasks, int ntask, int L,
+                                                 int nlines, const LineOp<float> &op0, const LineOp<float> &op1,
+                                                 int tid, int nthr, int skip) {
+    run_sweep_tasks<H, PC>(sm, tasks, ntask, L, nlines, op0, op1, tid, nthr, skip);
 }
 template <int H, int PC>
 __device__ __forceinline__ void run_sweep_tasks(const Smem<double> &sm, const Task *tasks, int ntask, int L,
@@ -880,13 +911,18 @@ __device__ __forceinline__ void run_sweep_tasks(const Smem<double> &sm, const Ta
 // Phase-A stores of task t's inputs at offset o: put1 for a task whose two
 // solves read one field, put2 for two fields.  In the pair layout both are
 // one 64-bit store (put1 stores the field in both lanes); in the planar
-// layout put1 stores the field once, in the first buffer.
+// layout put1 stores the field in both of the task's buffers (each solve runs
+// in place), or in its one buffer where the task's last buffer is the tile's
+// last (a one-field task).
 __device__ __forceinline__ void put1(const SmemPair &sm, int t, int o, float v) { sm.pair(t)[o] = make_float2(v, v); }
 __device__ __forceinline__ void put2(const SmemPair &sm, int t, int o, float v0, float v1) {
     sm.pair(t)[o] = make_float2(v0, v1);
 }
 template <typename T>
-__device__ __forceinline__ void put1(const Smem<T> &sm, int t, int o, T v) { sm.at(2 * t, o) = v; }
+__device__ __forceinline__ void put1(const Smem<T> &sm, int t, int o, T v) {
+    sm.at(2 * t, o) = v;
+    if (2 * t + 1 < sm.nbuf) sm.at(2 * t + 1, o) = v;
+}
 template <typename T>
 __device__ __forceinline__ void put2(const Smem<T> &sm, int t, int o, T v0, T v1) {
     sm.at(2 * t, o) = v0;
