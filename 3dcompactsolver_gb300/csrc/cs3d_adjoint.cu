@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(apply_threads<T>()) k_apply(ApplyArgs<T> a) {
             }
         });
     __syncthreads();
-    run_sweep_tasks<H, 0>(sm, tasks, np, L, t.nlines, a.op0, a.op1, threadIdx.x, blockDim.x);
+    // FP64: one solve per thread, each task in place in its own buffer
+    run_sweep_solves<H, 0>(sm, tasks, np, L, t.nlines, a.op0, a.op1, (int)threadIdx.x, (int)blockDim.x, -1);
     __syncthreads();
     if constexpr (F64IO) {
         struct Out64 { Pt pt; double e[kApplyMax]; };
