@@ -621,7 +621,8 @@ __global__ void __launch_bounds__(128) k_line_op(LineOpArgs a) {
         sm.b(0)[n * P + l] = a.in[(l0 + l) * N + n];
     }
     __syncthreads();
-    run_tasks<double, H>(sm, kTaskLone, 1, L, nl, a.op, a.op);
+    // one solve per line (the task's duplicate second solve left out)
+    run_sweep_solves<H, 0>(sm, kTaskLone, 1, L, nl, a.op, a.op, (int)threadIdx.x, (int)blockDim.x);
     __syncthreads();
     for (int p = threadIdx.x; p < N * L; p += blockDim.x) {
         Pt q;

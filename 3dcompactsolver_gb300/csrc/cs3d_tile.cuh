@@ -34,238 +34,25 @@ __device__ __forceinline__ void boundary_rows(const T *src, int P, const LineOp<
     }
 }
 
-// Two line solves, A and B, run interleaved by one thread.  Each reads its
-// line from s* (stride P) and writes the uncorrected solution to d*, which may
-// alias s*: the forward pass reads positions beyond the rows it writes, and
-// the boundary rows are formed before any write.  B may also read A's source
-// (1st and 2nd derivative of one field: A in place, B into its own buffer).
-// The Sherman-Morrison factor of a periodic line is formed in FP64 from the
-// line's end values and stored to f* in the work precision.
-template <typename T, int H, int PC = 0>
-__device__ __forceinline__ void solve_pair(const T *sa, T *da, const LineOp<T> &oa, T *fa, const T *sb, T *db,
-                                           const LineOp<T> &ob, T *fb, int P_) {
-    constexpr int W = 2 * H + 1;
-    // PC > 0: the buffer pitch as a compile-time constant, so that every
-    // shared-memory access of a chunk is a base register plus an immediate
-    const int P = PC > 0 ? PC : P_;
-    const int N = oa.N;
-    T pa[2 * H], pb[2 * H];
-    boundary_rows<T, H>(sa, P, oa, pa);
-    boundary_rows<T, H>(sb, P, ob, pb);
-    T ta[W], tb[W];
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-        ta[k] = oa.taps[kMaxH - H + k];
-        tb[k] = ob.taps[kMaxH - H + k];
-    }
-    const T *__restrict__ ma = oa.m;
-    const T *__restrict__ mb = ob.m;
-    // window of the first interior row H: positions 0..2H
-    T wa[W], wb[W];
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-        wa[k] = sa[k * P];
-        wb[k] = sb[k * P];
-    }
-    // rows 0..H-1
-    T ya = pa[0], yb = pb[0];
-    da[0] = ya;
-    db[0] = yb;
-#pragma unroll
-    for (int n = 1; n < H; ++n) {
-        ya = fma(-ldc(&ma[n]), ya, pa[n]);
-        yb = fma(-ldc(&mb[n]), yb, pb[n]);
-        da[n * P] = ya;
-        db[n * P] = yb;
-    }
-    // interior rows H..N-H-1 in chunks of kU, next chunk prefetched.  Chunks
-    // inside [klo, khi) of both operators (chunk starts kept on the kU
-    // lattice from H, so the 128-bit factor loads stay aligned) run on the
-    // register constants km; the others load m through mf.
-    const int nend = N - H;
-    int n = H;
-    const int klo = max(oa.klo, ob.klo), khi = min(oa.khi, ob.khi);
-    const int clo = H + kU * ((max(klo - H, 0) + kU - 1) / kU);
-    const T kma = oa.km, kmb = ob.km;
-    T na[kU], nb[kU], mna[kU], mnb[kU];
-#pragma unroll
-    for (int j = 0; j < kU; ++j) {
-        const int pos = n + H + 1 + j;
-        na[j] = sa[pos * P];
-        nb[j] = sb[pos * P];
-    }
-    load4(oa.mf, mna);
-    load4(ob.mf, mnb);
-    auto fwd_chunk = [&](auto kconst) {
-        constexpr bool K = decltype(kconst)::value;
-        T ca[kU], cb[kU], mca[kU], mcb[kU];
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            ca[j] = na[j]; cb[j] = nb[j];
-            mca[j] = K ? kma : mna[j];
-            mcb[j] = K ? kmb : mnb[j];
-        }
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            const int pos = n + kU + H + 1 + j;
-            na[j] = sa[pos * P];
-            nb[j] = sb[pos * P];
-        }
-        if (!K) {
-            load4(oa.mf + (n + kU - H), mna);
-            load4(ob.mf + (n + kU - H), mnb);
-        }
-        T ea[W + kU], eb[W + kU];
-#pragma unroll
-        for (int k = 0; k < W; ++k) { ea[k] = wa[k]; eb[k] = wb[k]; }
-#pragma unroll
-        for (int j = 0; j < kU; ++j) { ea[W + j] = ca[j]; eb[W + j] = cb[j]; }
-        T ra[kU], rb[kU];
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            T acc_a = T(0), acc_b = T(0);
-#pragma unroll
-            for (int k = 0; k < W; ++k) {
-                acc_a = fma(ta[k], ea[j + k], acc_a);
-                acc_b = fma(tb[k], eb[j + k], acc_b);
-            }
-            ra[j] = acc_a;
-            rb[j] = acc_b;
-        }
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            ya = fma(-mca[j], ya, ra[j]);
-            yb = fma(-mcb[j], yb, rb[j]);
-            da[(n + j) * P] = ya;
-            db[(n + j) * P] = yb;
-        }
-#pragma unroll
-        for (int k = 0; k < W; ++k) { wa[k] = ea[kU + k]; wb[k] = eb[kU + k]; }
-    };
-    // (the plain FP64 form keeps one loop: the constants' registers would
-    // cost it a resident block per SM, and its time is FP64 arithmetic)
-    if constexpr (sizeof(T) == 4) {
-        for (; n + kU <= nend && n < clo; n += kU) fwd_chunk(std::false_type{});
-        if (n + kU <= khi) {
-#pragma unroll 2
-            for (; n + kU <= nend && n + kU <= khi; n += kU) fwd_chunk(std::true_type{});
-            load4(oa.mf + (n - H), mna);
-            load4(ob.mf + (n - H), mnb);
-        }
-    }
-#pragma unroll 2
-    for (; n + kU <= nend; n += kU) fwd_chunk(std::false_type{});
-    for (; n < nend; ++n) {
-        T acc_a = T(0), acc_b = T(0);
-#pragma unroll
-        for (int k = 0; k < W; ++k) {
-            acc_a = fma(ta[k], wa[k], acc_a);
-            acc_b = fma(tb[k], wb[k], acc_b);
-        }
-        ya = fma(-ldc(&ma[n]), ya, acc_a);
-        yb = fma(-ldc(&mb[n]), yb, acc_b);
-#pragma unroll
-        for (int k = 0; k < W - 1; ++k) { wa[k] = wa[k + 1]; wb[k] = wb[k + 1]; }
-        const int pos = n + H + 1;
-        wa[W - 1] = pos < N ? sa[pos * P] : T(0);
-        wb[W - 1] = pos < N ? sb[pos * P] : T(0);
-        da[n * P] = ya;
-        db[n * P] = yb;
-    }
-    // rows N-H..N-1
-#pragma unroll
-    for (int b = 0; b < H; ++b) {
-        const int r = N - H + b;
-        ya = fma(-ldc(&ma[r]), ya, pa[H + b]);
-        yb = fma(-ldc(&mb[r]), yb, pb[H + b]);
-        da[r * P] = ya;
-        db[r * P] = yb;
-    }
-    // back substitution in chunks of kU, next chunk prefetched
-    const T *__restrict__ ca_ = oa.c;
-    const T *__restrict__ cb_ = ob.c;
-    const T *__restrict__ ia = oa.iw;
-    const T *__restrict__ ib = ob.iw;
-    T xa = ya * ldc(&ia[N - 1]);
-    T xb = yb * ldc(&ib[N - 1]);
-    da[(N - 1) * P] = xa;
-    db[(N - 1) * P] = xb;
-    const T xla = xa, xlb = xb;
-    n = N - 2;
-    T ya4[kU], yb4[kU], cA[kU], cB[kU], iA[kU], iB[kU];
-#pragma unroll
-    for (int j = 0; j < kU; ++j) {
-        const int r = max(n - j, 0);
-        ya4[j] = da[r * P]; yb4[j] = db[r * P];
-    }
-    load4(oa.cbk, cA); load4(ob.cbk, cB);
-    load4(oa.ibk, iA); load4(ob.ibk, iB);
-    // chunk tops on the lattice N-2-kU*k; chunks wholly inside [klo, khi)
-    // run on the constants kc, kiw
-    const T kca = oa.kc, kcb = ob.kc, kia = oa.kiw, kib = ob.kiw;
-    auto bwd_chunk = [&](auto kconst) {
-        constexpr bool K = decltype(kconst)::value;
-        T y0a[kU], y0b[kU], c0a[kU], c0b[kU], i0a[kU], i0b[kU];
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            y0a[j] = ya4[j]; y0b[j] = yb4[j];
-            c0a[j] = K ? kca : cA[j];
-            c0b[j] = K ? kcb : cB[j];
-            i0a[j] = K ? kia : iA[j];
-            i0b[j] = K ? kib : iB[j];
-        }
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            const int r = max(n - kU - j, 0);
-            ya4[j] = da[r * P]; yb4[j] = db[r * P];
-        }
-        if (!K) {
-            const int kb = N - 2 - (n - kU);
-            load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
-            load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
-        }
-#pragma unroll
-        for (int j = 0; j < kU; ++j) {
-            xa = fma(-c0a[j], xa, y0a[j]) * i0a[j];
-            xb = fma(-c0b[j], xb, y0b[j]) * i0b[j];
-            da[(n - j) * P] = xa;
-            db[(n - j) * P] = xb;
-        }
-    };
-    if constexpr (sizeof(T) == 4) {
-        for (; n - kU + 1 >= 0 && n >= khi; n -= kU) bwd_chunk(std::false_type{});
-        if (n - kU + 1 >= klo) {
-#pragma unroll 2
-            for (; n - kU + 1 >= klo; n -= kU) bwd_chunk(std::true_type{});
-            const int kb = N - 2 - n;
-            load4(oa.cbk + kb, cA); load4(ob.cbk + kb, cB);
-            load4(oa.ibk + kb, iA); load4(ob.ibk + kb, iB);
-        }
-    }
-#pragma unroll 2
-    for (; n - kU + 1 >= 0; n -= kU) bwd_chunk(std::false_type{});
-    for (; n >= 0; --n) {
-        xa = fma(-ldc(&ca_[n]), xa, da[n * P]) * ldc(&ia[n]);
-        xb = fma(-ldc(&cb_[n]), xb, db[n * P]) * ldc(&ib[n]);
-        da[n * P] = xa;
-        db[n * P] = xb;
-    }
-    *fa = oa.periodic ? (T)((to_f64(xa) + oa.bog * to_f64(xla)) * oa.inv_den) : T(0);
-    *fb = ob.periodic ? (T)((to_f64(xb) + ob.bog * to_f64(xlb)) * ob.inv_den) : T(0);
-}
-
 // ---------------------------------------------------------------------
-// FP32 line solves on pair-interleaved lines (the FP32-mixed sweeps)
+// line solves of the sweeps
 // ---------------------------------------------------------------------
-// The two solves of a task keep their lines pair-interleaved in shared
+// One compact-operator line solve (`solve_lanes`): the explicit right-hand
+// side formed on the fly from a sliding register window, the Thomas forward
+// pass and back substitution over the precomputed factors, in place (the
+// forward pass reads rows beyond those it writes, and the first and last H
+// explicit rows are formed before any write); for a periodic line the
+// Sherman-Morrison factor is formed in FP64 from the solution's end values and
+// stored for the consumers, which apply the correction on read.
+// FP32-mixed tiles keep the two solves of a task pair-interleaved in shared
 // memory: element n of the pair is the float2 at row n, lane x holding solve
-// A's line and lane y solve B's.  Each solve reads its own lane and writes it
-// in place (where both solves differentiate one field, the load phase stores
-// the field in both lanes).  A task runs on two threads, one lane each
-// (NL = 1: a warp's 32 lanes read 16 lines x 2 lanes, 128 contiguous bytes a
-// row), or on one thread that takes both lanes with 64-bit accesses (NL = 2).
-// The arithmetic is per lane, the operations and their order those of
-// solve_pair, so every form gives the same bits.
+// A's line and lane y solve B's, each solve reading and writing its own lane
+// (where both solves differentiate one field, the load phase stores the field
+// in both lanes).  A task runs on two threads, one lane each (NL = 1: a warp's
+// 32 lanes read 16 lines x 2 lanes, 128 contiguous bytes a row), or on one
+// thread that takes both lanes with 64-bit accesses (NL = 2).  The plain FP64
+// tiles are planar, one buffer per solve (NL = 1, RS = 1).  The arithmetic is
+// per solve and its order fixed, so every form gives the same bits.
 template <int NL, typename S = float>
 struct Lanes;
 template <>
@@ -327,8 +114,10 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL, S>::V *pr, const 
         y = Ls::fma_(Ls::mk(-ldc(&ma[n]), -ldc(&mb[n])), y, Ls::mk(pa[n], pb[n]));
         pr[n * P] = y;
     }
-    // interior rows H..N-H-1 in chunks of kU (as solve_pair: chunks inside
-    // [klo, khi) of both operators on the register constants)
+    // interior rows H..N-H-1 in chunks of kU, the next chunk read ahead;
+    // chunks inside [klo, khi) of both operators (chunk starts kept on the kU
+    // lattice from H, so the 128-bit factor loads stay aligned) run on the
+    // register constants km, the others load m through mf
     const int nend = N - H;
     int n = H;
     const int klo = max(oa.klo, ob.klo), khi = min(oa.khi, ob.khi);
@@ -458,7 +247,7 @@ __device__ __forceinline__ void solve_lanes(typename Lanes<NL, S>::V *pr, const 
 
 // Row n of the explicit right-hand side of a line read from src (stride P):
 // the interior stencil, or the explicit boundary row (wrapped columns), with
-// the products summed in the same order as solve_pair.
+// the products summed in the same order as solve_lanes.
 template <typename T, int H>
 __device__ __forceinline__ T rhs_row(const T *src, int P, const LineOp<T> &op, int n) {
     const int N = op.N;
@@ -484,7 +273,7 @@ __device__ __forceinline__ T rhs_row(const T *src, int P, const LineOp<T> &op, i
 // load their factors; rows inside run on the register constants km, kiw, kc
 // in chunks of kU with the next chunk's values read ahead (reads past the
 // body stay inside the line).  The operations and their order are those of
-// solve_pair, so the results are the same bit for bit.
+// solve_lanes, so the results are the same bit for bit.
 template <typename T, int PC>
 __device__ __forceinline__ void thomas_inplace(T *d, const LineOp<T> &op, T *fac, int P_) {
     const int P = PC > 0 ? PC : P_;
@@ -831,30 +620,9 @@ struct Task {
     signed char a, da, oa, b, db, ob;
 };
 
-// PC > 0: the caller has checked that the buffer pitch sm.P equals PC.
-template <typename T, int H, int PC = 0>
-__device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
-                                          const LineOp<T> &op0, const LineOp<T> &op1, int tid, int nthr) {
-    for (int w = tid; w < ntask * L; w += nthr) {
-        const int t = w / L, l = w - t * L;
-        if (l >= nlines) continue;
-        const Task tk = tasks[t];
-        const LineOp<T> &oa = tk.oa == 1 ? op1 : op0;
-        const LineOp<T> &ob = tk.ob == 1 ? op1 : op0;
-        solve_pair<T, H, PC>(sm.b(tk.a) + l, sm.b(tk.da) + l, oa, &sm.fact[tk.da * L + l], sm.b(tk.b) + l,
-                             sm.b(tk.db) + l, ob, &sm.fact[tk.db * L + l], sm.P);
-    }
-}
-template <typename T, int H, int PC = 0>
-__device__ __forceinline__ void run_tasks(const Smem<T> &sm, const Task *tasks, int ntask, int L, int nlines,
-                                          const LineOp<T> &op0, const LineOp<T> &op1) {
-    run_tasks<T, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, (int)threadIdx.x, (int)blockDim.x);
-}
-
 // The tasks of a sweep tile; sweep task t solves into buffers 2t and 2t+1.
 // FP32-mixed: one lane of the pair-interleaved layout per thread, the lane
-// whose destination buffer is `skip` (a task's unused duplicate) left out;
-// FP64: solve_pair on the planar layout.
+// whose destination buffer is `skip` (a task's unused duplicate) left out.
 template <int H, int PC>
 __device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *tasks, int ntask, int L, int nlines,
                                                 const LineOp<float> &op0, const LineOp<float> &op1, int tid,
@@ -878,8 +646,7 @@ __device__ __forceinline__ void run_sweep_tasks(const SmemPair &sm, const Task *
 // The plain FP64 sweeps' solves: one solve per thread, in place in its
 // destination buffer (the load phase stores a field whose two solves read it
 // in both of its task's buffers), the duplicate solve of a one-field task
-// left out; the arithmetic of solve_pair, so the same bits.  The mixed form
-// is run_sweep_tasks.
+// left out.  The mixed form is run_sweep_tasks.
 template <int H, int PC>
 __device__ __forceinline__ void run_sweep_solves(const Smem<double> &sm, const Task *tasks, int ntask, int L,
                                                  int nlines, const LineOp<double> &op0, const LineOp<double> &op1,
@@ -900,12 +667,6 @@ __device__ __forceinline__ void run_sweep_solves(const SmemPair &sm, const Task 
                                                  int nlines, const LineOp<float> &op0, const LineOp<float> &op1,
                                                  int tid, int nthr, int skip) {
     run_sweep_tasks<H, PC>(sm, tasks, ntask, L, nlines, op0, op1, tid, nthr, skip);
-}
-template <int H, int PC>
-__device__ __forceinline__ void run_sweep_tasks(const Smem<double> &sm, const Task *tasks, int ntask, int L,
-                                                int nlines, const LineOp<double> &op0, const LineOp<double> &op1,
-                                                int tid, int nthr, int = -1) {
-    run_tasks<double, H, PC>(sm, tasks, ntask, L, nlines, op0, op1, tid, nthr);
 }
 
 // Phase-A stores of task t's inputs at offset o: put1 for a task whose two
