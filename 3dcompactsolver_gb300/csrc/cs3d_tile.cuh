@@ -727,12 +727,6 @@ __device__ __forceinline__ Zn<T> zn(const LineOp<T> &d1, const LineOp<T> &d2, in
     z.z2 = d2.periodic ? ldc(&d2.z[n]) : T(0);
     return z;
 }
-// Corrected solution of buffer k at point p, with z the operator's vector.
-template <typename T>
-__device__ __forceinline__ T gz(const Smem<T> &sm, int k, const Pt &p, int L, T z) {
-    return fma(-sm.fact[k * L + p.l], z, sm.b(k)[p.o]);
-}
-
 // ---------------------------------------------------------------------
 // primitives of one point (IdealGas.hpp:49-80)
 // ---------------------------------------------------------------------
