@@ -117,11 +117,11 @@ def shear_layer(Nx=256, Ny=128, Nz=42, seed=0, du=0.6, delta=2.0, h=0.5,
     y faces with a sponge over sponge_frac of Ly next to each wall, TVD-RK3.
 
     rho = 1 and p = 1/gamma (sound speed 1), the state of the reference's
-    shear-layer driver (3DCompact.cpp:221-222) and the pressure its sponge
+    shear-layer case program (3DCompact.cpp:221-222) and the pressure its sponge
     relaxes toward (SpongeBC.hpp:56-58); U = (du/2) tanh((y - Ly/2)/delta),
-    the profile of 3DCompact.cpp:223 with the driver's du = 0.6 (:117), so the
+    the profile of 3DCompact.cpp:223 with that program's du = 0.6 (:117), so the
     free streams run at Mach du/2 = 0.3.  mu_ref, alphaF and the filter
-    interval are the driver's (:61, :90-91).  Seeded random velocity
+    interval are that program's (:61, :90-91).  Seeded random velocity
     perturbations of amplitude perturb*du/2 under the Gaussian window
     exp(-(y - Ly/2)^2) of 3DCompact.cpp:199-206.  The reference allows one BC
     kind per face, so the walls are ADIABATIC_WALL faces and the sponge is

@@ -30,8 +30,8 @@
 // of the device state.  syncToHost() fills q1, qk and q2 (rho1.., rhok..,
 // rho2..); it runs after setInitialConditions(), on every checkStep-th step
 // (when the reference's checkSolution reads them) and when the run ends.
-// syncToDevice() writes q1 back after a driver has changed it.  rho0..W0 are
-// allocated by initializeSolverData() for the driver to fill and freed by
+// syncToDevice() writes q1 back after the case program has changed it.  rho0..W0 are
+// allocated by initializeSolverData() for the case program to fill and freed by
 // setInitialConditions(), as the reference does (CSolver_AWS.cpp:124-128,
 // 219-224).  derivX..filtZ stay null: the reference's CPU operators are not
 // built; use Derivatives_GB300 / Filter_GB300.  Errors throw

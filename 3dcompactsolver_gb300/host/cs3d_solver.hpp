@@ -95,7 +95,7 @@ class CSolver_GB300 {
   public:
     int rkStep = 1;
     bool rkLast = false, endFlag = false, useTiming = false;
-    // initial conditions, written by the driver before setInitialConditions()
+    // initial conditions, written by the case program before setInitialConditions()
     std::vector<double> rho0v, p0v, U0v, V0v, W0v;
     double *rho0, *p0, *U0, *V0, *W0;
     // host mirrors of the conserved state (AbstractCSolver.hpp:19-26)
