@@ -213,7 +213,7 @@ class Solver:
         check(lib().cs3d_tgv_quantities(self.h, _dptr(out)))
         return out
 
-    # -- discrete adjoint (periodic, RK4, fixed dt, FP64) -------------------
+    # -- discrete adjoint (periodic, RK4 or TVD-RK3, fixed dt) ----------------
     def _q5(self, q):
         a = np.ascontiguousarray(q, dtype=np.float64).reshape(-1)
         if a.size != 5 * self.cfg.npts:

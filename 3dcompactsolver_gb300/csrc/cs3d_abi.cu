@@ -1588,7 +1588,6 @@ static int adj_check(cs3d_handle *h) {
         if (h->cfg.bc_type[d] != CS3D_PERIODIC_SOLVE)
             return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only (direction %d)", d);
     if (h->sponge || h->wall_faces) return fail(CS3D_ERR_STATE, "the adjoint is built for periodic boundaries only");
-    if (h->cfg.rk != CS3D_RK4) return fail(CS3D_ERR_STATE, "the adjoint is built for RK4");
     return CS3D_OK;
 }
 
@@ -1909,6 +1908,32 @@ static int adj_back(cs3d_handle *h, int fts, bool filtered, const T *const yin[4
                 return rc;
         }
     }
+    if (h->cfg.rk == CS3D_TVDRK3) {
+        // TVD-RK3 (TVDRK3.hpp:38-96) in reverse: y2 = y1 + dt R(y1),
+        // y3 = 3/4 y1 + 1/4 y2 + 1/4 dt R(y2), q+ = 1/3 y1 + 2/3 y3 + 2/3 dt R(y3)
+        // with y1 = q.  ybar3 = 2/3 qbar+ + J(y3)^T (2/3 dt qbar+) in YS,
+        // ybar2 = 1/4 ybar3 + J(y2)^T (dt/4 ybar3) in LAM, and
+        // qbar = 1/3 qbar+ + 3/4 ybar3 + ybar2 + J(y1)^T (dt ybar2); each
+        // cotangent lam is formed in the VJP kernel, the last VJP added into
+        // qbar by the chain-rule kernel.
+        double **LAM = h->adj_f[ADJ_LAM];
+        VjpFuse f3;
+        f3.qb2 = QB2;
+        f3.ca = 2.0 * dt / 3.0;
+        if ((rc = adj_vjp_tape<T>(h, yin[2], tapes[2], nullptr, YT, f3))) return rc;
+        if ((rc = adj_lin(h, YS, 2.0 / 3.0, QB2, 1.0, YT))) return rc;
+        VjpFuse f2;
+        f2.qb2 = YS;
+        f2.ca = 0.25 * dt;
+        if ((rc = adj_vjp_tape<T>(h, yin[1], tapes[1], nullptr, YT, f2))) return rc;
+        if ((rc = adj_lin(h, LAM, 0.25, YS, 1.0, YT))) return rc;
+        if ((rc = adj_lin(h, QB, 1.0 / 3.0, QB2, 0.75, YS, 1.0, LAM))) return rc;
+        VjpFuse f1;
+        f1.qb2 = LAM;
+        f1.ca = dt;
+        f1.acc = QB;
+        return adj_vjp_tape<T>(h, yin[0], tapes[0], nullptr, YT, f1);
+    }
     // RK4 (RK4.hpp:35-118) in reverse: q+ = q + dt/6 (k1 + 2 k2 + 2 k3 + k4),
     // y2 = q + dt/2 k1, y3 = q + dt/2 k2, y4 = q + dt k3, k_s = R(y_s)
     const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};  // weight of k_s in q+
@@ -1930,7 +1955,7 @@ static int adj_back(cs3d_handle *h, int fts, bool filtered, const T *const yin[4
 }
 
 // Adjoint of one time step taken from the state q0 with counters (ts, fts):
-// the four stages run again with their sweeps writing the stage tapes, then
+// the stages run again with their sweeps writing the stage tapes, then
 // adj_back.  T is the work type: the stage Jacobians are transposed in T at
 // the stage inputs the forward used (FP64 q1, qk; or, in the mixed form, the
 // FP32 shadows q1s, qks); the adjoint state and the filter transpose stay FP64.
@@ -1939,22 +1964,22 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
     int rc;
     double **Y[3] = {h->adj_f[ADJ_Y2], h->adj_f[ADJ_Y3], h->adj_f[ADJ_Y4]};
     const size_t n = (size_t)h->g.npts;
-    // stage inputs y1 = q0, y2, y3, y4 of the forward step, in T
+    // stage inputs y1 = q0, y2, y3 (, y4) of the forward step, in T
     const T *yin[4][5];
     h->timeStep = ts;
     h->filterTimeStep = fts;
     if ((rc = adj_set_state(h, q0))) return rc;
     for (int f = 0; f < 5; f++) yin[0][f] = sizeof(T) == 8 ? (const T *)q0[f] : (const T *)h->q1s[f];
     if ((rc = cs3d_pre_step(h))) return rc;
-    // the four stages again: their sweeps write the stage tapes (the values
-    // the stage's right-hand side was formed from), and stages 1-3 give the
-    // inputs y2, y3, y4 of the next
-    for (int st = 1; st <= 4; st++) {
+    // the stages again: their sweeps write the stage tapes (the values the
+    // stage's right-hand side was formed from), and every stage but the last
+    // gives the input of the next
+    for (int st = 1; st <= h->nstages; st++) {
         for (int i = 0; i < 48; i++) h->tape_out[i] = h->adj_tapes[st - 1][i];
         rc = run_stage<T>(h, st, 0);
         for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
         if (rc) return rc;
-        if (st == 4) break;
+        if (st == h->nstages) break;
         for (int f = 0; f < 5; f++) {
             const void *src = sizeof(T) == 8 ? (const void *)h->qk.f[f] : (const void *)h->qks[f];
             CS3D_CUDA(cudaMemcpyAsync(Y[st - 1][f], src, n * sizeof(T), cudaMemcpyDeviceToDevice, h->stream));
@@ -1966,14 +1991,14 @@ static int adj_step(cs3d_handle *h, int ts, int fts, double *const q0[5]) {
 }
 
 // Segment mode: one full time step from the current state (as cs3d_step)
-// with the sweeps writing the tapes of its four stages, and the stage inputs
-// copied, into slot j of the segment storage.
+// with the sweeps writing the tapes of its stages, and the stage inputs
+// copied, into slot j of the segment storage (four stage slots a step).
 template <typename T>
 static int adj_taped_step(cs3d_handle *h, int j) {
     int rc;
     const size_t fb = (size_t)h->g.npts * sizeof(T);
     if ((rc = cs3d_pre_step(h))) return rc;
-    for (int st = 1; st <= 4; st++) {
+    for (int st = 1; st <= h->nstages; st++) {
         char *yb = h->adj_segyin + (size_t)((j * 4 + st - 1) * 5) * fb;
         for (int f = 0; f < 5; f++) {
             const void *src = st == 1 ? (sizeof(T) == 8 ? (const void *)h->q1.f[f] : (const void *)h->q1s[f])
@@ -1982,7 +2007,7 @@ static int adj_taped_step(cs3d_handle *h, int j) {
         }
         char *tb = h->adj_segtape + (size_t)((j * 4 + st - 1) * 48) * fb;
         for (int i = 0; i < 48; i++) h->tape_out[i] = tb + i * fb;
-        rc = run_stage<T>(h, st, st == 4);
+        rc = run_stage<T>(h, st, st == h->nstages);
         for (int i = 0; i < 48; i++) h->tape_out[i] = nullptr;
         if (rc) return rc;
     }

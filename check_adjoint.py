@@ -1,9 +1,9 @@
 """Check the discrete adjoint on the Taylor-Green vortex.
 
-    python check_adjoint.py --N 128 --steps 200 --dirs 16
+    python check_adjoint.py --N 128 --steps 200 --dirs 16 [--rk tvdrk3]
 
-J = volume-averaged kinetic energy after `steps` RK4 steps at a fixed time
-step (the CFL 0.5 step of the initial state).  The gradient dJ/d(U0, V0, W0)
+J = volume-averaged kinetic energy after `steps` RK4 (or TVD-RK3) steps at a
+fixed time step (the CFL 0.5 step of the initial state).  The gradient dJ/d(U0, V0, W0)
 from cs3d_adjoint_backward (FP64 handle, and FP32-mixed handle) is compared
 on `dirs` seeded random directions with central differences of the FP64
 forward, and the mixed gradient with the FP64 gradient.  Prints one JSON
@@ -69,9 +69,11 @@ def main(argv=None):
     ap.add_argument("--eps", type=float, default=1e-5)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--rk", default="rk4", choices=["rk4", "tvdrk3"])
     args = ap.parse_args(argv)
     N, steps = args.N, args.steps
-    cfg, ic = cases.tgv(N)
+    rk = cs3d.TVDRK3_KIND if args.rk == "tvdrk3" else cs3d.RK4_KIND
+    cfg, ic = cases.tgv(N, rk=rk)
     s = cs3d.Solver(cfg)
     s.set_initial_conditions(*ic)
     s.step()
@@ -79,7 +81,8 @@ def main(argv=None):
     s.close()
     cfg.dt_fixed = dt
     rho0, p0, U0, V0, W0 = ic
-    out = {"workload": f"tgv{N}", "steps": steps, "dt_fixed": dt, "dirs": args.dirs, "eps": args.eps}
+    out = {"workload": f"tgv{N}", "rk": args.rk, "steps": steps, "dt_fixed": dt, "dirs": args.dirs,
+           "eps": args.eps}
     g64, J64, trec, tback = adjoint(cfg, ic, steps, args.every)
     out["J"] = J64
     out["fp64"] = {"record_s": trec, "backward_s": tback,
@@ -87,7 +90,7 @@ def main(argv=None):
     gU, gV, gW = cs3d.ic_velocity_gradient(g64, rho0, U0, V0, W0)
     gm = None
     if not args.no_mixed:
-        cfg_m, _ = cases.tgv(N, precision=cs3d.FP32_MIXED)
+        cfg_m, _ = cases.tgv(N, precision=cs3d.FP32_MIXED, rk=rk)
         cfg_m.dt_fixed = dt
         gm_q, Jm, trec_m, tback_m = adjoint(cfg_m, ic, steps, args.every)
         out["mixed"] = {"record_s": trec_m, "backward_s": tback_m, "J": Jm,

@@ -291,12 +291,12 @@ int cs3d_load_solution(cs3d_handle *h, const char *prefix, int time_step, double
 /* ---- discrete adjoint of the time steps --------------------------------
  * No counterpart in the reference.  Gradient of an objective J of the state
  * after n steps with respect to the state before them, by the transposed
- * (discrete adjoint) step: filter^T, then the four RK4 stages in reverse,
+ * (discrete adjoint) step: filter^T, then the RK stages in reverse,
  * each J^T lam of the stage right-hand side through the transposed compact
  * operators (D1^T = -D1, D2^T = D2, F^T = F on periodic grids), the
  * generated pointwise adjoint of the flux and viscous terms and the chain
  * rule through the ideal-gas primitives.  Scope: periodic boundaries, RK4
- * and a fixed time step (cfg.dt_fixed > 0).  On a CS3D_FP64 handle every
+ * or TVD-RK3, and a fixed time step (cfg.dt_fixed > 0).  On a CS3D_FP64 handle every
  * operation is FP64; on a CS3D_FP32_MIXED handle the stage Jacobians are
  * transposed in FP32 at the FP32 stage inputs of the mixed forward, while
  * the adjoint state, the RK combination and the filter transpose are FP64.

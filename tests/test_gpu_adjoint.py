@@ -11,7 +11,9 @@ FP64 forward (the same product path, fixed time step).
 * the checkpoint interval does not change the gradient, and the solver is
   back at its recorded final state afterwards;
 * the backward from the tapes kept by the segment replay equals, bit for
-  bit, the one that recomputes each step's stages.
+  bit, the one that recomputes each step's stages;
+* the same for TVD-RK3 steps (differences, segment storage, the mixed
+  adjoint against the FP64 one).
 """
 import numpy as np
 import pytest
@@ -80,10 +82,11 @@ def _forward_J(gpu_pkg, cfg, ic, nsteps):
     return J
 
 
-@pytest.mark.parametrize("filter_step,every", [(1, 4), (2, 0)])
-def test_adjoint_matches_finite_differences(gpu_pkg, cases, filter_step, every):
+@pytest.mark.parametrize("filter_step,every,rk", [(1, 4, "rk4"), (2, 0, "rk4"), (2, 4, "tvdrk3")])
+def test_adjoint_matches_finite_differences(gpu_pkg, cases, filter_step, every, rk):
     N, nsteps = 16, 6
-    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=filter_step)
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=filter_step,
+                            rk=gpu_pkg.TVDRK3_KIND if rk == "tvdrk3" else gpu_pkg.RK4_KIND)
     rho0, p0, U0, V0, W0 = ic
     s = gpu_pkg.Solver(cfg)
     s.set_initial_conditions(*ic)
@@ -124,17 +127,18 @@ def test_adjoint_checkpointing_and_restore(gpu_pkg, cases):
     assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[0], grads[2])
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_adjoint_segment_storage_equals_recompute(gpu_pkg, cases, mixed):
+@pytest.mark.parametrize("mixed,rk", [(False, "rk4"), (True, "rk4"), (False, "tvdrk3"), (True, "tvdrk3")])
+def test_adjoint_segment_storage_equals_recompute(gpu_pkg, cases, mixed, rk):
     """The backward from the tapes and stage inputs kept by the segment replay
     gives the same bits as the per-step recompute of each step's stages
     (OPT_ADJ_RECOMPUTE): 7 steps in segments of 3 (one ragged), filter every
-    second step, FP64 and FP32-mixed handles."""
+    second step, FP64 and FP32-mixed handles, RK4 and TVD-RK3."""
     N, nsteps = 16, 7
-    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=2)
+    rkc = gpu_pkg.TVDRK3_KIND if rk == "tvdrk3" else gpu_pkg.RK4_KIND
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=2, rk=rkc)
     if mixed:
         dt = cfg.dt_fixed
-        cfg, _ = cases.tgv(N, filter_step=2, precision=gpu_pkg.FP32_MIXED)
+        cfg, _ = cases.tgv(N, filter_step=2, precision=gpu_pkg.FP32_MIXED, rk=rkc)
         cfg.dt_fixed = dt
     out = []
     for recompute in (0, 1):
@@ -250,3 +254,24 @@ def test_mixed_rhs_vjp_tracks_fp64(gpu_pkg, cases):
     b = m.rhs_vjp(q, w)
     for f in range(5):
         assert np.abs(a[f] - b[f]).max() <= 2e-3 * np.abs(a[f]).max(), f
+
+
+def test_mixed_tvdrk3_adjoint_tracks_fp64(gpu_pkg, cases):
+    """TVD-RK3 (TVDRK3.hpp:38-96): the FP32-mixed adjoint's velocity gradient
+    within 1e-6 of the FP64 adjoint's in relative L2 (TGV 24^3, 8 steps,
+    filter every second step)."""
+    N, nsteps = 24, 8
+    cfg, ic = _tgv_fixed_dt(gpu_pkg, cases, N, filter_step=2, rk=gpu_pkg.TVDRK3_KIND)
+    cfg_m, _ = cases.tgv(N, precision=gpu_pkg.FP32_MIXED, filter_step=2, rk=gpu_pkg.TVDRK3_KIND)
+    cfg_m.dt_fixed = cfg.dt_fixed
+    grads = []
+    for c in (cfg, cfg_m):
+        s = gpu_pkg.Solver(c)
+        s.set_initial_conditions(*ic)
+        s.adjoint_record(nsteps, 3)
+        g, _ = s.adjoint_backward(gpu_pkg.ADJ_KE_MEAN)
+        grads.append(gpu_pkg.ic_velocity_gradient(g, ic[0], ic[2], ic[3], ic[4]))
+        s.close()
+    num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(grads[1], grads[0])))
+    gnorm = np.sqrt(sum(np.sum(b * b) for b in grads[0]))
+    assert gnorm > 0 and num / gnorm <= 1e-6, num / gnorm
