@@ -6,7 +6,8 @@ J = volume-averaged kinetic energy after `steps` RK4 (or TVD-RK3) steps at a
 fixed time step (the CFL 0.5 step of the initial state).  The gradient dJ/d(U0, V0, W0)
 from cs3d_adjoint_backward (FP64 handle, and FP32-mixed handle) is compared
 on `dirs` seeded random directions with central differences of the FP64
-forward, and the mixed gradient with the FP64 gradient.  Prints one JSON
+forward, and the mixed gradient with the FP64 gradient; each direction's
+conditioning |g.d| / (|g| |d|) is reported with it.  Prints one JSON
 line: per-direction relative errors, their maxima, and the time of the record
 (forward with checkpoints) and of the backward sweep.
 """
@@ -100,7 +101,8 @@ def main(argv=None):
         den = np.sqrt(sum(np.sum(b * b) for b in (gU, gV, gW)))
         out["mixed"]["grad_rel_l2_vs_fp64"] = float(num / den)
     rng = np.random.default_rng(args.seed)
-    e64, em = [], []
+    e64, em, cond = [], [], []
+    gnorm = np.sqrt(sum(np.sum(b * b) for b in (gU, gV, gW)))
     t0 = time.perf_counter()
     for d in range(args.dirs):
         dU, dV, dW = (smooth_direction(rng, N) for _ in range(3))
@@ -110,12 +112,15 @@ def main(argv=None):
         fd = (Jp - Jm_) / (2 * eps)
         a64 = float(np.sum(gU * dU + gV * dV + gW * dW))
         e64.append(abs(a64 - fd) / abs(fd))
+        # |g.d| / (|g| |d|): how well the direction determines g.d
+        cond.append(abs(a64) / (gnorm * np.sqrt(np.sum(dU * dU) + np.sum(dV * dV) + np.sum(dW * dW))))
         if gm is not None:
             am = float(np.sum(gm[0] * dU + gm[1] * dV + gm[2] * dW))
             em.append(abs(am - fd) / abs(fd))
     out["fd_s"] = time.perf_counter() - t0
     out["fp64"]["fd_rel_err"] = e64
     out["fp64"]["fd_rel_err_max"] = max(e64)
+    out["direction_conditioning"] = cond
     if gm is not None:
         out["mixed"]["fd_rel_err"] = em
         out["mixed"]["fd_rel_err_max"] = max(em)
