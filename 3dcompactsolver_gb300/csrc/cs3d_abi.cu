@@ -573,6 +573,7 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
     double cp = h->gas.R * h->gas.gamma / (h->gas.gamma - 1.0);
     h->gas.cpPr = cp / 0.7;
     h->gas.mu_ref = cfg->mu_ref;
+    h->gas.iR = 1.0 / h->gas.R;
     h->nstages = cfg->rk == CS3D_TVDRK3 ? 3 : 4;
     h->mixed = cfg->precision == CS3D_FP32_MIXED;
     h->tb = h->mixed ? 4 : 8;
@@ -714,7 +715,8 @@ static int launch_cfl_reduce(cs3d_handle *h) {
     if (h->mixed)
         for (int f = 0; f < 5; f++) a.qs[f] = h->q1s[f];
     a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
-    a.idx = (float)(1.0 / h->dx); a.idy = (float)(1.0 / h->dy); a.idz = (float)(1.0 / h->dz);
+    a.idx64 = 1.0 / h->dx; a.idy64 = 1.0 / h->dy; a.idz64 = 1.0 / h->dz;
+    a.idx = (float)a.idx64; a.idy = (float)a.idy64; a.idz = (float)a.idz64;
     a.max_out = h->scal + 2;
     a.nan_flag = h->flag;
     tstart(h, CS3D_K_CFL);

@@ -28,6 +28,7 @@ struct GasParams {
     double R;       // p_ref / rho_ref / T_ref
     double cpPr;    // cp / Pr
     double mu_ref;
+    double iR;      // 1 / R
 };
 
 // What the z sweep writes as the FP32 shadow of the next stage's input.
@@ -122,6 +123,7 @@ struct CflArgs {
     double dx, dy, dz;
     float idx, idy, idz;  // mixed: 1/dx, 1/dy, 1/dz (formed on the host: an FP64
                           // division per thread costs more than the whole read)
+    double idx64, idy64, idz64;  // the same in FP64 for the plain form
     double *max_out;
     int *nan_flag;
 };

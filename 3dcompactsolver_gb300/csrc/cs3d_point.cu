@@ -152,11 +152,13 @@ __global__ void k_cfl(CflArgs a) {
     } else {
         for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < a.g.npts;
              gi += (long long)gridDim.x * blockDim.x) {
-            const double r = a.q.f[0][gi];
-            const double U = a.q.f[1][gi] / r, V = a.q.f[2][gi] / r, W = a.q.f[3][gi] / r;
+            // one reciprocal of rho and the host's 1/dx, 1/dy, 1/dz instead of
+            // seven FP64 divisions (within an ulp of the quotients)
+            const double r = a.q.f[0][gi], ir = __drcp_rn(r);
+            const double U = a.q.f[1][gi] * ir, V = a.q.f[2][gi] * ir, W = a.q.f[3][gi] * ir;
             const double p = a.gas.gm1 * (a.q.f[4][gi] - 0.5 * r * (U * U + V * V + W * W));
-            const double c = sqrt(a.gas.gamma * p / r);
-            const double v = (fabs(U) + c) / a.dx + (fabs(V) + c) / a.dy + (fabs(W) + c) / a.dz;
+            const double c = sqrt(a.gas.gamma * p * ir);
+            const double v = (fabs(U) + c) * a.idx64 + (fabs(V) + c) * a.idy64 + (fabs(W) + c) * a.idz64;
             bad |= !(v == v) || isinf(v);
             mx = fmax(mx, v);
         }

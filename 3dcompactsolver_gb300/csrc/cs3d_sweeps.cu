@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? kMinBloc
             const unsigned gi = p.gi;
             const Zn<T> zz = zn(a.d1, a.d2, p.n);
             const T U = in.v[0], V = in.v[1], W = in.v[2], Tt = in.v[3];
-            const T mu = muref * pow(Tt, (T)0.76);
+            const T mu = muref * visc_pow(Tt);
             const T amu = (T)0.76 * mu / Tt;
             a.mu[gi] = mu;
             a.amu[gi] = amu;

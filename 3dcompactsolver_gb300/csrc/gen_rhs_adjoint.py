@@ -108,7 +108,7 @@ def emit(path):
         for i, n in enumerate(NAMES):
             lines.append(f"    const T {'Tt' if n == 'T' else n} = in[{i}];")
         lines.append("    const T c13 = T(1.0 / 3.0), c43 = T(4.0 / 3.0), c23 = T(2.0 / 3.0);")
-        lines.append("    const T mu = muref * pow(Tt, (T)0.76);")
+        lines.append("    const T mu = muref * visc_pow(Tt);")
         lines.append("    const T amu = (T)0.76 * mu / Tt;")
         lines.append("    (void)c23;")
         return lines
