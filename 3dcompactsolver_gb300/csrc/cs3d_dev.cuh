@@ -143,14 +143,15 @@ __device__ __forceinline__ int faces_of(const Geom &g, int i, int j, int k) {
 }
 
 // T^0.76, the exponent of the viscosity law mu = mu_ref T^0.76 (IdealGas.hpp).
-// FP32: the library powf.  FP64, whose pipe issues two operations per SM and
+// FP32: exp2(0.76 log2 T) with the hardware log2 (absolute error about 2^-22,
+// so about 1.5e-7 relative in the result: an FP32 rounding).  FP64, whose pipe issues two operations per SM and
 // clock: y^25 = T^19 solved by one step of Halley's method (cubic
 // convergence) from an FP32 estimate exp2(0.76 log2 T) (relative error below
 // 2e-6), written as the correction y + y (c - a) / (13 a + 12 c) with
 // a = y^25, c = T^19 by repeated squaring: about 20 FP64 operations and one
 // division, within 2 ulp of the library pow for T in [0.01, 1000] (sampled
 // against it).  Outside [1e-6, 1e6], and for NaN, the library pow.
-__device__ __forceinline__ float visc_pow(float T) { return powf(T, 0.76f); }
+__device__ __forceinline__ float visc_pow(float T) { return exp2f(0.76f * __log2f(T)); }
 __device__ __forceinline__ double visc_pow(double T) {
     if (!(T > 1e-6 && T < 1e6)) return pow(T, 0.76);
     const double y = (double)exp2f(0.76f * log2f((float)T));

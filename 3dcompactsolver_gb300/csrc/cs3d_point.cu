@@ -116,10 +116,13 @@ __device__ __forceinline__ void block_max_commit(double mx, double *out) {
     }
 }
 
+// kShadow: the mixed form's FP32 shadow, else the FP64 state (two instances:
+// the FP64 branch's registers would otherwise cost the FP32 pass occupancy)
+template <bool kShadow>
 __global__ void k_cfl(CflArgs a) {
     double mx = 0.0;
     int bad = 0;
-    if (a.qs[0]) {
+    if constexpr (kShadow) {
         // FP32 shadow: four consecutive points per thread (128-bit loads of
         // the 16-byte aligned arrays), one reciprocal of rho per point
         float fm = 0.f;
@@ -395,7 +398,8 @@ cudaError_t launch_wall_pre(const BCArgs &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 cudaError_t launch_cfl(const CflArgs &a, cudaStream_t s) {
-    k_cfl<<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    if (a.qs[0]) k_cfl<true><<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
+    else k_cfl<false><<<grid_for(a.g.npts, 256), 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 cudaError_t launch_nan_scan(const CflArgs &a, cudaStream_t s) {

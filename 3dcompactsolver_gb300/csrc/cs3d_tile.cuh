@@ -740,8 +740,8 @@ __device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2
     PrimW<T> s;
     s.ru = r1; s.rv = r2; s.rw = r3; s.re = r4;
     if constexpr (sizeof(T) == 8) {
-        // one reciprocal of rho instead of four FP64 divisions (within an ulp
-        // of the quotients)
+        // one correctly rounded reciprocal of rho instead of four FP64
+        // divisions (within an ulp of the quotients)
         const double ir = __drcp_rn(r0);
         s.U = r1 * ir;
         s.V = r2 * ir;
@@ -749,6 +749,9 @@ __device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2
         s.p = gp.gm1 * (r4 - 0.5 * r0 * (s.U * s.U + s.V * s.V + s.W * s.W));
         s.Tt = s.p * ir * gp.iR;
     } else {
+        // FP32 keeps the quotients: the reciprocal's rounding, shared by the
+        // points of a region of near-uniform density, doubled the mixed
+        // form's error in the shear layer's fluctuation statistics
         s.U = r1 / r0;
         s.V = r2 / r0;
         s.W = r3 / r0;
