@@ -573,7 +573,6 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
     double cp = h->gas.R * h->gas.gamma / (h->gas.gamma - 1.0);
     h->gas.cpPr = cp / 0.7;
     h->gas.mu_ref = cfg->mu_ref;
-    h->gas.iR = 1.0 / h->gas.R;
     h->nstages = cfg->rk == CS3D_TVDRK3 ? 3 : 4;
     h->mixed = cfg->precision == CS3D_FP32_MIXED;
     h->tb = h->mixed ? 4 : 8;

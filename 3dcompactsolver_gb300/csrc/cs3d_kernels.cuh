@@ -28,7 +28,6 @@ struct GasParams {
     double R;       // p_ref / rho_ref / T_ref
     double cpPr;    // cp / Pr
     double mu_ref;
-    double iR;      // 1 / R
 };
 
 // What the z sweep writes as the FP32 shadow of the next stage's input.

@@ -747,7 +747,7 @@ __device__ __forceinline__ PrimW<T> prim_w(const GasParams &gp, T r0, T r1, T r2
         s.V = r2 * ir;
         s.W = r3 * ir;
         s.p = gp.gm1 * (r4 - 0.5 * r0 * (s.U * s.U + s.V * s.V + s.W * s.W));
-        s.Tt = s.p * ir * gp.iR;
+        s.Tt = s.p * ir * (1.0 / gp.R);  // 1/R: invariant, formed once per thread
     } else {
         // FP32 keeps the quotients: the reciprocal's rounding, shared by the
         // points of a region of near-uniform density, doubled the mixed
