@@ -151,7 +151,12 @@ int cs3d_set_field(cs3d_handle *h, int field, const double *host_in);
 /* The conserved state q1 (rho1, rhoU1, rhoV1, rhoW1, rhoE1; AbstractCSolver.hpp:
  * 19-26) between host and device in one call: the five copies are queued
  * together and waited for once.  Same result as cs3d_get_field /
- * cs3d_set_field on fields 0..4. */
+ * cs3d_set_field on fields 0..4.  Setting the state leaves the CFL maximum
+ * of the state the last step ended with, from which the next cs3d_pre_step
+ * takes dt -- as the reference's calcDtFromCFL reads the primitive arrays of
+ * its last updateNonConservedData (CSolver_AWS.cpp:507-525, 1895-1935), not
+ * arrays written since; cs3d_set_initial_conditions and cs3d_load_solution
+ * form it from the new state. */
 int cs3d_get_conserved(cs3d_handle *h, double *const host_out[5]);
 int cs3d_set_conserved(cs3d_handle *h, const double *const host_in[5]);
 /* Device pointer of a field (XYZ layout, FP64), valid until destroy. */
