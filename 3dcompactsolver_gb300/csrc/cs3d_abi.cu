@@ -516,6 +516,11 @@ static int pick_L(size_t tb, int nbuf, int N, int pitch_plus, int budget_kb = 72
     return L;
 }
 
+// The sweeps' shared-memory pitch beyond the tile width: one pad column in
+// the mixed form's x tiles (their points walk along a line first), none in
+// the FP64 x tiles (points across the lines first) nor in y and z.
+static int x_pitch_plus(const cs3d_handle *h, int d) { return d == 0 && h->mixed ? 1 : 0; }
+
 // Sponge strength sigma (SpongeBC.hpp:64-150) with sigma starting at zero.
 static void build_sigma(const cs3d_config *c, std::vector<double> &sig, int *any) {
     const int Nx = c->Nx, Ny = c->Ny, Nz = c->Nz;
@@ -636,15 +641,21 @@ extern "C" int cs3d_create(const cs3d_config *cfg, cs3d_handle **out) {
             if (r) return fail_free(r);
         }
     for (int d = 0; d < 3; d++) {
-        // Tile shape.  Default: the widest tile within 75 kB for x (3 blocks
-        // of 256 per SM), 72 kB for y and z (2 blocks of 256).  A mixed-form y or z tile
+        // Tile shape.  Default: the widest tile within 75 kB for the mixed
+        // x sweep (3 blocks of 256 per SM), 72 kB for y and z (2 blocks of
+        // 256).  A mixed-form y or z tile
         // narrower than 16 lines there (z rows of 32 bytes or less per field)
         // instead takes one block of 512 threads per SM and the widest tile
         // within 200 kB: measured at 128^3, z 0.79 -> 0.70 ms per step; where
         // the 72 kB tile is already 16 lines wide (N = 42) one block per SM was
         // slower, its phases no longer overlapping another block's.
         const int nb = sweep_nbuf(d, (int)h->tb);
-        h->L[d] = pick_L(h->tb, nb, Nd[d], d == 0 ? 1 : 0, d == 0 ? 75 : 72, true);
+        h->L[d] = pick_L(h->tb, nb, Nd[d], x_pitch_plus(h, d), d == 0 ? (h->mixed ? 75 : 115) : 72, true);
+        // FP64 x: at most 4 lines within 115 kB (2 blocks per SM at N = 256,
+        // 3 at 128, registers).  Against the former 75 kB tiles with a pad
+        // column (1 line at N = 256): HIT 256^3 x 51.7 -> 26.3 ms per step,
+        // shear layer 3.25 -> 1.84; 8 lines at 128^3 measured 4% slower.
+        if (!h->mixed && d == 0 && h->L[d] > 4) h->L[d] = 4;
         h->threads[d] = h->mixed ? (d == 0 ? sweep_threads<float>(0) : 256) : sweep_threads<double>(d);
         if (h->mixed && d > 0 && h->L[d] < 16) {
             h->L[d] = pick_L(h->tb, nb, Nd[d], 0, 200, true);
@@ -903,7 +914,7 @@ static int run_stage(cs3d_handle *h, int st, int last) {
         a.L = h->L[d];
         a.lgL = ilog2(a.L);
         a.divN = make_fastdiv((unsigned)(d == 0 ? h->g.Nx : d == 1 ? h->g.Ny : h->g.Nz));
-        a.P = a.L + (d == 0 ? 1 : 0);
+        a.P = a.L + x_pitch_plus(h, d);
         if (sizeof(T) == 8) {
             a.d1 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][0].op);
             a.d2 = *reinterpret_cast<const LineOp<T> *>(&h->op64[d][1].op);

@@ -78,11 +78,13 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? kMinBloc
     const int N = t.N, NL = N * L;
     const auto sm = SweepSmem<T>::at(smem_raw, sizeof(T) == 4 ? XNB2 : XNB, L, P, N);
     const GasParams gp = a.gas;
+    // FP64 tiles: points across the lines first, pitch P = L (no pad column)
+    constexpr bool kXLineFirst = sizeof(T) == 8;
     // phase A: primitives and the inputs of the x-solves
     struct InA { Pt pt; T q[5]; };
     batched<InA, sizeof(T) == 4 ? 4 : 2>(NL,
         [&](InA &in, int p) {
-            in.pt = point<0>(t, p, L, P, a.lgL, a.divN);
+            in.pt = point<0, kXLineFirst>(t, p, L, P, a.lgL, a.divN);
 #pragma unroll
             for (int f = 0; f < 5; ++f) in.q[f] = a.qs[f][in.pt.gi];
         },
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(sweep_threads<T>(0), sizeof(T) == 4 ? kMinBloc
     struct InC { Pt pt; T v[4]; };
     batched<InC, sizeof(T) == 4 ? 4 : 2>(NL,
         [&](InC &in, int p) {
-            in.pt = point<0>(t, p, L, P, a.lgL, a.divN);
+            in.pt = point<0, kXLineFirst>(t, p, L, P, a.lgL, a.divN);
             const unsigned gi = in.pt.gi;
             in.v[0] = a.prim[0][gi]; in.v[1] = a.prim[1][gi]; in.v[2] = a.prim[2][gi]; in.v[3] = a.prim[4][gi];
         },

@@ -419,10 +419,16 @@ struct Pt {
     bool ok;
 };
 
-template <int DIR>
+// Point p of a tile: LF false walks along a line first (x tiles of the mixed
+// form: a warp's loads cover contiguous x; the shared-memory pitch P = L + 1
+// keeps the transposed stores off common banks); LF true walks across the
+// tile's lines first (y and z tiles, whose lines are adjacent in memory, and
+// the FP64 x tiles: 8-byte elements give each line a 32- or 64-byte run per
+// warp, whole sectors, and the stores are then conflict-free at P = L).
+template <int DIR, bool LF = (DIR != 0)>
 __device__ __forceinline__ Pt point(const Tile &t, int p, int L, int P, int lgL, FastDiv dv) {
     Pt q;
-    if (DIR == 0) {
+    if (!LF) {
         q.l = (int)((__umulhi((unsigned)p, dv.mul) + (unsigned)p) >> dv.sh);
         q.n = p - q.l * t.N;
     } else {
