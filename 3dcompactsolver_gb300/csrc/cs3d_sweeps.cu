@@ -177,8 +177,10 @@ __constant__ Task kTasksY2[8] = {{YU, YU, 0, YU, YU2, 1}, {YV, YV, 0, YV, YV2, 1
                                  {YRV, YRV, 0, YF1, YF1, 0}, {YF2, YF2, 0, YF3, YF3, 0},
                                  {YF4, YF4, 0, YF4, YDUM, 0}};
 
+// FP64: 3 blocks per SM (168 registers, no spills): 2.93 -> 2.67 ms per step at
+// TGV 128^3, 37.5 -> 27.1 at HIT 256^3, the same bits
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? kMinBlocksY : 2) k_sweep_y(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(1), sizeof(T) == 4 ? kMinBlocksY : 3) k_sweep_y(SweepArgs<T> a) {
     const int L = a.L, P = PC > 0 ? PC : a.P;
     const Tile t = make_tile<1>(a.g, L);
     const int N = t.N, NL = N * L;
@@ -499,8 +501,10 @@ struct ZSweep {
     }
 };
 
+// FP64: 3 blocks per SM (168 registers; 88 bytes of spill stores): 4.70 ->
+// 4.52 ms per step at TGV 128^3, 52.5 -> 44.9 at HIT 256^3, the same bits
 template <typename T, int PC>
-__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? kMinBlocksZ : 2) k_sweep_z(SweepArgs<T> a) {
+__global__ void __launch_bounds__(sweep_threads<T>(2), sizeof(T) == 4 ? kMinBlocksZ : 3) k_sweep_z(SweepArgs<T> a) {
     const Tile t = make_tile<2>(a.g, a.L);
     const auto sm = SweepSmem<T>::at(smem_raw, ZNB, a.L, PC > 0 ? PC : a.P, t.N);
     ZSweep<T, PC>::load(a, t, sm, threadIdx.x, blockDim.x);
