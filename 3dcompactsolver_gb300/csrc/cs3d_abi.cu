@@ -724,7 +724,6 @@ static int launch_cfl_reduce(cs3d_handle *h) {
     a.q = h->q1;
     if (h->mixed)
         for (int f = 0; f < 5; f++) a.qs[f] = h->q1s[f];
-    a.dx = h->dx; a.dy = h->dy; a.dz = h->dz;
     a.idx64 = 1.0 / h->dx; a.idy64 = 1.0 / h->dy; a.idz64 = 1.0 / h->dz;
     a.idx = (float)a.idx64; a.idy = (float)a.idy64; a.idz = (float)a.idz64;
     a.max_out = h->scal + 2;

@@ -119,7 +119,6 @@ struct CflArgs {
     GasParams gas;
     Q5 q;
     const float *qs[5];   // mixed: the FP32 shadow of q1 instead of q
-    double dx, dy, dz;
     float idx, idy, idz;  // mixed: 1/dx, 1/dy, 1/dz (formed on the host: an FP64
                           // division per thread costs more than the whole read)
     double idx64, idy64, idz64;  // the same in FP64 for the plain form
